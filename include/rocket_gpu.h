@@ -1,0 +1,141 @@
+/*
+ * rocket_gpu.h — C ABI of the GB300 pocketfft transform path.
+ *
+ * The ten `numba_*` entry points keep the names, argument order and argument types of the
+ * reference's C shim rocket_fft/_pocketfft_numba.cpp (cited per function below), so the
+ * reference's Numba intrinsics (rocket_fft/pocketfft.py:32-128) can bind them unchanged.
+ * Array arguments use numba's array-struct layout; shapes are element counts and strides are
+ * BYTES, as in the reference. `data` may be a device pointer (CUDA allocation, managed or
+ * device memory) or a host pointer; host arrays are staged through device memory on the
+ * current stream and the call returns after the result is back on the host.
+ *
+ * The reference returns void and reports nothing (its C++ exceptions cross the C ABI, which is
+ * undefined behaviour). Here every void entry point records a status and message that
+ * rocketgpu_last_status()/rocketgpu_last_error() return for the calling thread, and every
+ * function has an `int`-returning `_st` twin. `nthreads` is accepted and ignored: the GPU grid
+ * replaces the reference's CPU thread pool.
+ */
+#ifndef ROCKET_GPU_H
+#define ROCKET_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* numba's array struct (numba/_arraystruct.h, not vendored by the reference either):
+ * shape_and_strides holds ndim extents followed by ndim byte strides. */
+typedef struct rocketgpu_arystruct {
+  void *meminfo;
+  void *parent;
+  int64_t nitems;
+  int64_t itemsize;
+  void *data;
+  int64_t shape_and_strides[1]; /* really [2 * ndim] */
+} rocketgpu_arystruct_t;
+
+/* status codes */
+#define RG_OK 0
+#define RG_ERR_ARG 1         /* bad shape, stride, axis, dtype or type argument */
+#define RG_ERR_UNSUPPORTED 2 /* valid request outside what this build implements */
+#define RG_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define RG_ERR_NOMEM 4       /* device memory exhausted */
+#define RG_ERR_INTERNAL 5
+
+/* ---- drop-in entry points (same signatures as the reference) ---- */
+
+/* rocket_fft/_pocketfft_numba.cpp:25-29 */
+uint64_t numba_good_size(uint64_t target, bool real);
+
+/* rocket_fft/_pocketfft_numba.cpp:31-49 (c2c), :91-109 (r2c), :111-143 (c2c_sym),
+ * :145-163 (c2r) */
+void numba_c2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+               rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+void numba_r2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+               rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+void numba_c2c_sym(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                   rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+void numba_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+               rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+
+/* rocket_fft/_pocketfft_numba.cpp:51-69 (dct), :71-89 (dst) */
+void numba_dct(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+               rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+               uint64_t nthreads);
+void numba_dst(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+               rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+               uint64_t nthreads);
+
+/* rocket_fft/_pocketfft_numba.cpp:165-183 */
+void numba_r2r_fftpack(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                       rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                       bool real2hermitian, bool forward, double fct, uint64_t nthreads);
+
+/* rocket_fft/_pocketfft_numba.cpp:185-203 (separable), :205-223 (genuine) */
+void numba_r2r_separable_hartley(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                 rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                                 double fct, uint64_t nthreads);
+void numba_r2r_genuine_hartley(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                               rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                               double fct, uint64_t nthreads);
+
+/* ---- status-returning twins (no reference counterpart: the reference returns void) ---- */
+int numba_c2c_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                 rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+int numba_r2c_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                 rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+int numba_c2c_sym_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                     rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, bool forward,
+                     double fct, uint64_t nthreads);
+int numba_c2r_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                 rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+int numba_dct_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                 rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+                 uint64_t nthreads);
+int numba_dst_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                 rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+                 uint64_t nthreads);
+int numba_r2r_fftpack_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                         rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                         bool real2hermitian, bool forward, double fct, uint64_t nthreads);
+int numba_r2r_separable_hartley_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                   rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                                   double fct, uint64_t nthreads);
+int numba_r2r_genuine_hartley_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                 rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                                 double fct, uint64_t nthreads);
+
+/* ---- runtime control (no reference counterpart) ---- */
+
+/* Status and message of the calling thread's most recent call (RG_OK / "" after success).
+ * rocketgpu_last_error copies at most len-1 bytes plus a terminating NUL and returns the
+ * status. */
+int rocketgpu_last_status(void);
+int rocketgpu_last_error(char *buf, size_t len);
+
+/* The CUDA stream (cudaStream_t) the calling thread's transforms are issued on; NULL is the
+ * legacy default stream. Device-array calls return without synchronising. */
+void rocketgpu_set_stream(void *stream);
+void *rocketgpu_get_stream(void);
+
+/* Plan cache: number of cached plans, device bytes they hold, and a clear that must not run
+ * concurrently with transforms. */
+uint64_t rocketgpu_plan_cache_entries(void);
+uint64_t rocketgpu_plan_cache_bytes(void);
+int rocketgpu_plan_cache_clear(void);
+
+/* Kernel launches issued by this library since load (all threads). */
+uint64_t rocketgpu_launch_count(void);
+
+/* Library version string. */
+const char *rocketgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ROCKET_GPU_H */

@@ -1,0 +1,30 @@
+"""rocket-fft_gb300: the pocketfft transform path of rocket-fft on NVIDIA GB300 (sm_103a).
+
+The low-level API keeps rocket-fft's names and semantics (``rocket_fft/__init__.py:18-34``)
+and runs every transform in hand-written CUDA kernels behind a C ABI
+(``include/rocket_gpu.h``). The directory name carries a hyphen, so import it through
+``importlib`` (see ``load_package`` in the tests and bench) under the name
+``rocket_fft_gb300``.
+"""
+
+from .pocketfft import (  # noqa: F401
+    TypingError,
+    c2c,
+    c2c_sym,
+    c2r,
+    dct,
+    dst,
+    good_size,
+    launch_count,
+    plan_cache_bytes,
+    plan_cache_clear,
+    plan_cache_entries,
+    r2c,
+    r2r_fftpack,
+    r2r_genuine_hartley,
+    r2r_separable_hartley,
+    set_stream,
+    version,
+)
+
+__version__ = "0.1.0"

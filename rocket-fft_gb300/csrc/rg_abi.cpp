@@ -1,0 +1,399 @@
+// extern "C" entry points: the drop-in replacement of rocket_fft/_pocketfft_numba.cpp.
+//
+// Each numba_* function parses numba array structs (shapes, BYTE strides), validates them,
+// stages host arrays through device memory when needed, and runs the N-d driver on the
+// calling thread's stream. Errors never escape as exceptions: they become a status code and
+// a thread-local message (rocketgpu_last_status / rocketgpu_last_error).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rocket_gpu.h"
+#include "rg_error.hpp"
+#include "rg_exec.hpp"
+#include "rg_launch.hpp"
+#include "rg_plan.hpp"
+
+#define RG_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+thread_local int t_status = RG_OK;
+thread_local std::string t_msg;
+thread_local cudaStream_t t_stream = nullptr;
+
+template <class F> int guarded(F &&f) {
+  try {
+    f();
+    t_status = RG_OK;
+    t_msg.clear();
+  } catch (const rg::Error &e) {
+    t_status = e.code;
+    t_msg = e.what();
+  } catch (const std::bad_alloc &) {
+    t_status = RG_ERR_NOMEM;
+    t_msg = "host allocation failed";
+  } catch (const std::exception &e) {
+    t_status = RG_ERR_INTERNAL;
+    t_msg = e.what();
+  } catch (...) {
+    t_status = RG_ERR_INTERNAL;
+    t_msg = "unknown error";
+  }
+  return t_status;
+}
+
+using rg::DType;
+using rg::Error;
+using rg::NdArray;
+
+struct Desc {
+  void *data;
+  int64_t itemsize;
+  std::vector<int64_t> shape, bstride;  // byte strides
+};
+
+Desc parse(uint64_t ndim, const rocketgpu_arystruct_t *a, const char *name) {
+  RG_CHECK(a != nullptr, RG_ERR_ARG, std::string(name) + " is NULL");
+  Desc d;
+  d.data = a->data;
+  d.itemsize = a->itemsize;
+  d.shape.resize(ndim);
+  d.bstride.resize(ndim);
+  for (uint64_t i = 0; i < ndim; ++i) {
+    d.shape[i] = a->shape_and_strides[i];
+    d.bstride[i] = a->shape_and_strides[ndim + i];
+    RG_CHECK(d.shape[i] >= 0, RG_ERR_ARG, std::string(name) + ": negative extent");
+  }
+  return d;
+}
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+bool any_zero(const std::vector<int64_t> &s) {
+  for (int64_t v : s)
+    if (v == 0) return true;
+  return false;
+}
+
+std::vector<uint64_t> parse_axes(const rocketgpu_arystruct_t *ax, uint64_t ndim) {
+  RG_CHECK(ax != nullptr, RG_ERR_ARG, "axes is NULL");
+  RG_CHECK(ax->itemsize == 8, RG_ERR_ARG, "axes must be a 64-bit integer array");
+  const int64_t n = ax->nitems;
+  RG_CHECK(n >= 0, RG_ERR_ARG, "bad axes size");
+  std::vector<uint64_t> axes(static_cast<size_t>(n));
+  if (n == 0) return axes;
+  const int64_t stride = ax->shape_and_strides[1];  // 1-D: [extent, byte stride]
+  const char *base = static_cast<const char *>(ax->data);
+  if (is_device_ptr(base)) {
+    std::vector<char> host(size_t((n - 1) * std::llabs(stride) + 8));
+    RG_CHECK(stride > 0, RG_ERR_ARG, "device axes must have a positive stride");
+    RG_CUDA(cudaMemcpy(host.data(), base, host.size(), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < n; ++i) std::memcpy(&axes[size_t(i)], host.data() + i * stride, 8);
+  } else {
+    for (int64_t i = 0; i < n; ++i) std::memcpy(&axes[size_t(i)], base + i * stride, 8);
+  }
+  for (uint64_t a : axes) RG_CHECK(a < ndim, RG_ERR_ARG, "bad axis number");
+  return axes;
+}
+
+// A device view of one argument: either the caller's device array, or a staged copy of a
+// host array (copied in on construction if `copy_in`, copied back by copy_out()).
+class Staged {
+ public:
+  Staged(const Desc &d, bool copy_in_always, cudaStream_t st) : d_(d), st_(st) {
+    for (size_t i = 0; i < d.shape.size(); ++i)
+      RG_CHECK(d.bstride[i] % d.itemsize == 0, RG_ERR_UNSUPPORTED,
+               "strides must be multiples of the item size");
+    view_.shape = d.shape;
+    view_.stride.resize(d.shape.size());
+    for (size_t i = 0; i < d.shape.size(); ++i) view_.stride[i] = d.bstride[i] / d.itemsize;
+    if (any_zero(d.shape) || d.data == nullptr) {
+      view_.data = d.data;
+      return;
+    }
+    device_ = is_device_ptr(d.data);
+    if (device_) {
+      RG_CHECK(reinterpret_cast<uintptr_t>(d.data) % uintptr_t(d.itemsize) == 0, RG_ERR_UNSUPPORTED,
+               "device data must be aligned to its item size");
+      view_.data = d.data;
+      return;
+    }
+    int64_t lo = 0, hi = 0, count = 1;
+    for (size_t i = 0; i < d.shape.size(); ++i) {
+      const int64_t ext = (d.shape[i] - 1) * d.bstride[i];
+      if (ext < 0) lo += ext; else hi += ext;
+      count *= d.shape[i];
+    }
+    span_lo_ = lo;
+    span_ = size_t(hi - lo + d.itemsize);
+    buf_.reset(new rg::DevBuf(span_, st));
+    view_.data = static_cast<char *>(buf_->get()) - lo;
+    const bool dense = span_ == size_t(count * d.itemsize);
+    if (copy_in_always || !dense)
+      RG_CUDA(cudaMemcpyAsync(buf_->get(), static_cast<char *>(d.data) + lo, span_,
+                              cudaMemcpyHostToDevice, st));
+  }
+  void copy_out() {
+    if (!buf_) return;
+    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(d_.data) + span_lo_, buf_->get(), span_,
+                            cudaMemcpyDeviceToHost, st_));
+  }
+  bool staged() const { return bool(buf_); }
+  const NdArray &view() const { return view_; }
+  // share another staged view's device memory when both describe the same host array
+  void alias(const Staged &o) {
+    view_.data = o.view_.data;
+    buf_.reset();
+    shared_ = true;
+  }
+  bool shared() const { return shared_; }
+
+ private:
+  Desc d_;
+  cudaStream_t st_;
+  NdArray view_;
+  bool device_ = false, shared_ = false;
+  int64_t span_lo_ = 0;
+  size_t span_ = 0;
+  std::unique_ptr<rg::DevBuf> buf_;
+};
+
+// Runs body(in_view, out_view) with host arrays staged, then copies results back.
+template <class Body>
+void with_views(const Desc &din, const Desc &dout, Body body) {
+  cudaStream_t st = t_stream;
+  Staged sin(din, true, st);
+  const bool inplace = din.data == dout.data && din.bstride == dout.bstride &&
+                       din.itemsize == dout.itemsize && sin.staged();
+  Staged sout(dout, false, st);
+  if (inplace) sout.alias(sin);
+  body(sin.view(), sout.view(), st);
+  if (sin.staged() || sout.staged()) {
+    if (inplace)
+      sin.copy_out();
+    else
+      sout.copy_out();
+    RG_CUDA(cudaStreamSynchronize(st));
+  }
+}
+
+void check_same_shape(const Desc &a, const Desc &b) {
+  RG_CHECK(a.shape == b.shape, RG_ERR_ARG, "input and output shapes differ");
+}
+
+void check_half_shape(const Desc &full, const Desc &half, const std::vector<uint64_t> &axes) {
+  RG_CHECK(full.shape.size() == half.shape.size(), RG_ERR_ARG, "rank mismatch");
+  const uint64_t last = axes.back();
+  for (size_t i = 0; i < full.shape.size(); ++i) {
+    const int64_t want = i == last ? full.shape[i] / 2 + 1 : full.shape[i];
+    RG_CHECK(half.shape[i] == want, RG_ERR_ARG,
+             "half-spectrum shape must equal the real shape with the last axis n/2+1");
+  }
+}
+
+DType complex_dtype(int64_t itemsize) {
+  RG_CHECK(itemsize == 8 || itemsize == 16, RG_ERR_ARG, "complex arrays must be complex64 or complex128");
+  return itemsize == 16 ? DType::F64 : DType::F32;
+}
+DType real_dtype(int64_t itemsize) {
+  RG_CHECK(itemsize == 4 || itemsize == 8, RG_ERR_ARG, "real arrays must be float32 or float64");
+  return itemsize == 8 ? DType::F64 : DType::F32;
+}
+
+int do_c2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+           rocketgpu_arystruct_t *axes, bool forward, double fct) {
+  return guarded([&] {
+    const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
+    const DType dt = complex_dtype(din.itemsize);
+    RG_CHECK(dout.itemsize == din.itemsize, RG_ERR_ARG, "input and output dtypes differ");
+    check_same_shape(din, dout);
+    const auto ax = parse_axes(axes, ndim);
+    if (any_zero(din.shape) || ax.empty()) return;
+    with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
+      rg::exec_c2c(dt, i, o, ax, forward, fct, st);
+    });
+  });
+}
+
+int do_r2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+           rocketgpu_arystruct_t *axes, bool forward, double fct, bool sym) {
+  return guarded([&] {
+    const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
+    const DType dt = real_dtype(din.itemsize);
+    RG_CHECK(dout.itemsize == 2 * din.itemsize, RG_ERR_ARG, "output must be the matching complex dtype");
+    const auto ax = parse_axes(axes, ndim);
+    RG_CHECK(!ax.empty(), RG_ERR_ARG, "at least one axis is required");
+    if (sym)
+      check_same_shape(din, dout);
+    else
+      check_half_shape(din, dout, ax);
+    if (any_zero(din.shape)) return;
+    with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
+      if (sym)
+        rg::exec_c2c_sym(dt, i, o, ax, forward, fct, st);
+      else
+        rg::exec_r2c(dt, i, o, ax, forward, fct, st);
+    });
+  });
+}
+
+int do_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+           rocketgpu_arystruct_t *axes, bool forward, double fct) {
+  return guarded([&] {
+    const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
+    const DType dt = complex_dtype(din.itemsize);
+    RG_CHECK(2 * dout.itemsize == din.itemsize, RG_ERR_ARG, "output must be the matching real dtype");
+    const auto ax = parse_axes(axes, ndim);
+    RG_CHECK(!ax.empty(), RG_ERR_ARG, "at least one axis is required");
+    check_half_shape(dout, din, ax);
+    if (any_zero(dout.shape)) return;
+    with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
+      rg::exec_c2r(dt, i, o, ax, forward, fct, st);
+    });
+  });
+}
+
+int not_yet(const char *what) {
+  return guarded([&] { throw Error(RG_ERR_UNSUPPORTED, std::string(what) + " is not available in this build"); });
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// drop-in entry points
+// ---------------------------------------------------------------------------------------
+
+RG_EXPORT uint64_t numba_good_size(uint64_t target, bool real) {
+  uint64_t r = 0;
+  guarded([&] { r = real ? rg::good_size_real(target) : rg::good_size_cmplx(target); });
+  return r;
+}
+
+RG_EXPORT int numba_c2c_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                           rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t) {
+  return do_c2c(ndim, ain, aout, axes, forward, fct);
+}
+RG_EXPORT void numba_c2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                         rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads) {
+  numba_c2c_st(ndim, ain, aout, axes, forward, fct, nthreads);
+}
+
+RG_EXPORT int numba_r2c_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                           rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t) {
+  return do_r2c(ndim, ain, aout, axes, forward, fct, false);
+}
+RG_EXPORT void numba_r2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                         rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads) {
+  numba_r2c_st(ndim, ain, aout, axes, forward, fct, nthreads);
+}
+
+RG_EXPORT int numba_c2c_sym_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                               rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, bool forward,
+                               double fct, uint64_t) {
+  return do_r2c(ndim, ain, aout, axes, forward, fct, true);
+}
+RG_EXPORT void numba_c2c_sym(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                             rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads) {
+  numba_c2c_sym_st(ndim, ain, aout, axes, forward, fct, nthreads);
+}
+
+RG_EXPORT int numba_c2r_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                           rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t) {
+  return do_c2r(ndim, ain, aout, axes, forward, fct);
+}
+RG_EXPORT void numba_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                         rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads) {
+  numba_c2r_st(ndim, ain, aout, axes, forward, fct, nthreads);
+}
+
+RG_EXPORT int numba_dct_st(uint64_t, const rocketgpu_arystruct_t *, rocketgpu_arystruct_t *,
+                           rocketgpu_arystruct_t *, uint64_t, double, bool, uint64_t) {
+  return not_yet("dct");
+}
+RG_EXPORT void numba_dct(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                         rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+                         uint64_t nthreads) {
+  numba_dct_st(ndim, ain, aout, axes, type, fct, ortho, nthreads);
+}
+RG_EXPORT int numba_dst_st(uint64_t, const rocketgpu_arystruct_t *, rocketgpu_arystruct_t *,
+                           rocketgpu_arystruct_t *, uint64_t, double, bool, uint64_t) {
+  return not_yet("dst");
+}
+RG_EXPORT void numba_dst(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                         rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+                         uint64_t nthreads) {
+  numba_dst_st(ndim, ain, aout, axes, type, fct, ortho, nthreads);
+}
+RG_EXPORT int numba_r2r_fftpack_st(uint64_t, const rocketgpu_arystruct_t *, rocketgpu_arystruct_t *,
+                                   rocketgpu_arystruct_t *, bool, bool, double, uint64_t) {
+  return not_yet("r2r_fftpack");
+}
+RG_EXPORT void numba_r2r_fftpack(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                 rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                                 bool real2hermitian, bool forward, double fct, uint64_t nthreads) {
+  numba_r2r_fftpack_st(ndim, ain, aout, axes, real2hermitian, forward, fct, nthreads);
+}
+RG_EXPORT int numba_r2r_separable_hartley_st(uint64_t, const rocketgpu_arystruct_t *,
+                                             rocketgpu_arystruct_t *, rocketgpu_arystruct_t *, double,
+                                             uint64_t) {
+  return not_yet("r2r_separable_hartley");
+}
+RG_EXPORT void numba_r2r_separable_hartley(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                           rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                                           double fct, uint64_t nthreads) {
+  numba_r2r_separable_hartley_st(ndim, ain, aout, axes, fct, nthreads);
+}
+RG_EXPORT int numba_r2r_genuine_hartley_st(uint64_t, const rocketgpu_arystruct_t *,
+                                           rocketgpu_arystruct_t *, rocketgpu_arystruct_t *, double,
+                                           uint64_t) {
+  return not_yet("r2r_genuine_hartley");
+}
+RG_EXPORT void numba_r2r_genuine_hartley(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                         rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
+                                         double fct, uint64_t nthreads) {
+  numba_r2r_genuine_hartley_st(ndim, ain, aout, axes, fct, nthreads);
+}
+
+// ---------------------------------------------------------------------------------------
+// runtime control
+// ---------------------------------------------------------------------------------------
+
+RG_EXPORT int rocketgpu_last_status(void) { return t_status; }
+
+RG_EXPORT int rocketgpu_last_error(char *buf, size_t len) {
+  if (buf && len > 0) {
+    const size_t n = std::min(len - 1, t_msg.size());
+    std::memcpy(buf, t_msg.data(), n);
+    buf[n] = '\0';
+  }
+  return t_status;
+}
+
+RG_EXPORT void rocketgpu_set_stream(void *stream) { t_stream = static_cast<cudaStream_t>(stream); }
+RG_EXPORT void *rocketgpu_get_stream(void) { return t_stream; }
+
+RG_EXPORT uint64_t rocketgpu_plan_cache_entries(void) { return rg::cache_entries(); }
+RG_EXPORT uint64_t rocketgpu_plan_cache_bytes(void) { return rg::cache_bytes(); }
+RG_EXPORT int rocketgpu_plan_cache_clear(void) {
+  return guarded([] {
+    rg::cache_clear();
+    rg::pool_trim();
+  });
+}
+
+RG_EXPORT uint64_t rocketgpu_launch_count(void) { return rg::launch_count(); }
+
+RG_EXPORT const char *rocketgpu_version(void) { return "rocket-fft_gb300 0.1.0 (sm_103a)"; }

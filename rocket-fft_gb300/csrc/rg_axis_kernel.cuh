@@ -1,0 +1,260 @@
+// The axis-job kernel: a batch of 1-D transforms along one axis of a strided array.
+//
+// One CTA owns TB rows (transforms). Phases, separated by barriers:
+//   1. row offsets:  decompose each row number over the batch dims (both sides)
+//   2. load:         global -> shared, coalesced either along the axis (rows are long and
+//                    contiguous) or across rows (rows are adjacent columns of a strided axis);
+//                    op-specific input conversion (real pairs, Hermitian half, chirp, sign)
+//   3. pre-op:       e.g. the c2r even-length Hermitian merge
+//   4. on-chip FFT:  Stockham radix passes (rg_fft.cuh)
+//   5. post-op:      e.g. the r2c even-length split, the Bluestein spectrum product + 2nd FFT
+//   6. store:        shared -> global with conjugation, scaling, four-step twiddles
+//
+// It replaces the reference's per-thread gather -> plan.exec -> scatter loop of general_nd /
+// general_r2c / general_c2r (rocket_fft/_pocketfft_hdronly.h:3568-3607, 3723-3852): rows
+// processed as SIMD lanes there are processed as CTA rows here.
+#pragma once
+#include "rg_fft.cuh"
+
+namespace rg {
+
+__device__ __forceinline__ int64_t side_offset(const Side &s, int64_t g) {
+  int64_t off = 0;
+  for (int d = 0; d < s.nbd; ++d) {
+    const int64_t q = g / s.bshape[d];
+    off += (g - q * s.bshape[d]) * s.bstride[d];
+    g = q;
+  }
+  return off;
+}
+
+// Map loop counter e to (row r, element i) for a row-major walk (i fastest) or a
+// column walk (r fastest).
+__device__ __forceinline__ void walk(int e, int colmap, int TB, const FastDiv &dTB, int units,
+                                     const FastDiv &dUnits, int &r, int &i) {
+  if (colmap) {
+    i = int(fdiv(uint32_t(e), dTB));
+    r = e - i * TB;
+  } else {
+    r = int(fdiv(uint32_t(e), dUnits));
+    i = e - r * units;
+  }
+}
+
+// W_N^t from the split table: lo[t & mask] * hi[t >> shift]
+template <typename T>
+__device__ __forceinline__ cx<T> split_twiddle(const cx<T> *__restrict__ lo, const cx<T> *__restrict__ hi,
+                                               int shift, uint32_t t) {
+  const cx<T> a = lo[t & ((1u << shift) - 1u)];
+  const cx<T> b = hi[t >> shift];
+  return mul<T>(a, b);
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs a, FastDiv dTB,
+                                                   FastDiv dIn, FastDiv dOut) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int TB = a.TB;
+  const int pitch = a.pitch, ps = a.ps;
+  cx<T> *sm = reinterpret_cast<cx<T> *>(smraw);           // ping-pong buffer 0 (loads land here)
+  cx<T> *sm1 = sm + size_t(TB) * pitch;                    // ping-pong buffer 1
+  int64_t *roff_in = reinterpret_cast<int64_t *>(smraw + 2 * sizeof(cx<T>) * size_t(TB) * pitch);
+  int64_t *roff_out = roff_in + TB;
+  int *rowaux = reinterpret_cast<int *>(roff_out + TB);
+
+  const int64_t row0 = int64_t(blockIdx.x) * TB;
+  const int rows = int(min(int64_t(TB), a.nrows - row0));
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
+  const T fct = T(a.fct);
+
+  for (int r = tid; r < rows; r += nth) {
+    roff_in[r] = side_offset(a.ld, row0 + r);
+    roff_out[r] = side_offset(a.st, row0 + r);
+    if (OP == OP_C2C_TW) rowaux[r] = int((row0 + r) % a.aux_n);
+  }
+  __syncthreads();
+
+  const int L = a.core.L;
+
+  // ---------------- load ----------------
+  {
+    const int units = a.nin;
+    const int total = TB * units;
+    const int64_t s = a.ld.axis_stride;
+    for (int e = tid; e < total; e += nth) {
+      int r, i;
+      walk(e, a.ld.colmap, TB, dTB, units, dIn, r, i);
+      if (r >= rows) continue;
+      const int64_t off = roff_in[r];
+      if constexpr (OP == OP_C2C || OP == OP_C2C_TW) {
+        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
+        cx<T> v = in[off + i * s];
+        if (cin) v.y = -v.y;
+        sm[sidx(r, i, pitch, ps)] = v;
+      } else if constexpr (OP == OP_BLUE) {
+        // a_j = x_j * conj(bk_j), zero-padded to L below
+        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
+        const cx<T> *bk = reinterpret_cast<const cx<T> *>(a.aux);
+        cx<T> v = in[off + i * s];
+        if (cin) v.y = -v.y;
+        sm[sidx(r, i, pitch, ps)] = mulc<T>(v, bk[i]);
+      } else if constexpr (OP == OP_R2C_EVEN) {
+        // units = n real values; pair 2j, 2j+1 becomes complex element j
+        const T *in = reinterpret_cast<const T *>(a.in);
+        const T v = in[off + i * s];
+        T *sr = reinterpret_cast<T *>(sm + r * pitch);
+        const int j = i >> 1;
+        sr[2 * (j + (j >> ps)) + (i & 1)] = v;
+      } else if constexpr (OP == OP_R2C_ODD) {
+        const T *in = reinterpret_cast<const T *>(a.in);
+        sm[sidx(r, i, pitch, ps)] = mk<T>(in[off + i * s], T(0));
+      } else if constexpr (OP == OP_C2R_EVEN) {
+        // units = L+1 Hermitian bins; imaginary parts of bins 0 and L are ignored
+        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
+        cx<T> v = in[off + i * s];
+        if (cin) v.y = -v.y;
+        if (i == 0 || i == L) v.y = T(0);
+        sm[sidx(r, i, pitch, ps)] = v;
+      } else if constexpr (OP == OP_C2R_ODD) {
+        // units = (n+1)/2 bins; build conj of the full Hermitian spectrum:
+        //   W_0 = Re X_0, W_i = conj(X_i), W_{n-i} = X_i
+        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
+        cx<T> v = in[off + i * s];
+        if (cin) v.y = -v.y;
+        if (i == 0) {
+          sm[sidx(r, 0, pitch, ps)] = mk<T>(v.x, T(0));
+        } else {
+          sm[sidx(r, i, pitch, ps)] = cj<T>(v);
+          sm[sidx(r, L - i, pitch, ps)] = v;
+        }
+      }
+    }
+    if constexpr (OP == OP_BLUE) {
+      // zero padding j in [n, L)
+      const int n = a.n;
+      const int padn = L - n;
+      for (int e = tid; e < TB * padn; e += nth) {
+        const int r = e / padn;
+        const int i = n + (e - r * padn);
+        if (r < rows) sm[sidx(r, i, pitch, ps)] = mk<T>(T(0), T(0));
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---------------- pre-op ----------------
+  if constexpr (OP == OP_C2R_EVEN) {
+    // Z_k = A + u, Z_{L-k} = conj(A - u), A = X_k + conj(X_{L-k}), B = X_k - conj(X_{L-k}),
+    // u = i * conj(W_n^k) * B; the core then transforms conj(Z).
+    const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);  // W_n^k, k = 0..L/2
+    const int half = L / 2 + 1;
+    for (int e = tid; e < TB * half; e += nth) {
+      const int r = e / half;
+      const int k = e - r * half;
+      if (r >= rows) continue;
+      if (k == 0) {
+        const cx<T> x0 = sm[sidx(r, 0, pitch, ps)], xl = sm[sidx(r, L, pitch, ps)];
+        const cx<T> A = add<T>(x0, cj<T>(xl)), B = sub<T>(x0, cj<T>(xl));
+        sm[sidx(r, 0, pitch, ps)] = cj<T>(add<T>(A, mposi<T>(B)));
+      } else {
+        const int kc = L - k;
+        const cx<T> xk = sm[sidx(r, k, pitch, ps)], xc = sm[sidx(r, kc, pitch, ps)];
+        const cx<T> A = add<T>(xk, cj<T>(xc)), B = sub<T>(xk, cj<T>(xc));
+        const cx<T> u = mposi<T>(mulc<T>(B, w[k]));
+        sm[sidx(r, k, pitch, ps)] = cj<T>(add<T>(A, u));
+        if (kc != k) sm[sidx(r, kc, pitch, ps)] = sub<T>(A, u);  // conj(conj(A - u))
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---------------- FFT ----------------
+  cx<T> *res = fft_rows<T>(sm, sm1, rows, pitch, ps, a.core);
+
+  // ---------------- post-op ----------------
+  if constexpr (OP == OP_R2C_EVEN) {
+    // X_k = E + t, X_{L-k} = conj(E - t), E = (Z_k + conj Z_{L-k})/2, O = (Z_k - conj Z_{L-k})/(2i),
+    // t = W_n^k O; X_0 = Re Z_0 + Im Z_0, X_L = Re Z_0 - Im Z_0.
+    const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
+    const int half = L / 2 + 1;
+    for (int e = tid; e < TB * half; e += nth) {
+      const int r = e / half;
+      const int k = e - r * half;
+      if (r >= rows) continue;
+      if (k == 0) {
+        const cx<T> z0 = res[sidx(r, 0, pitch, ps)];
+        res[sidx(r, 0, pitch, ps)] = mk<T>(z0.x + z0.y, T(0));
+        res[sidx(r, L, pitch, ps)] = mk<T>(z0.x - z0.y, T(0));
+      } else {
+        const int kc = L - k;
+        const cx<T> zk = res[sidx(r, k, pitch, ps)], zc = cj<T>(res[sidx(r, kc, pitch, ps)]);
+        const cx<T> E = scl<T>(add<T>(zk, zc), T(0.5));
+        const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
+        const cx<T> t = mul<T>(w[k], O);
+        res[sidx(r, k, pitch, ps)] = add<T>(E, t);
+        if (kc != k) res[sidx(r, kc, pitch, ps)] = cj<T>(sub<T>(E, t));
+      }
+    }
+    __syncthreads();
+  } else if constexpr (OP == OP_BLUE) {
+    // C = conj(A * bkf); then forward FFT again gives conj(conv)
+    const cx<T> *bkf = reinterpret_cast<const cx<T> *>(a.aux2);
+    for (int e = tid; e < TB * L; e += nth) {
+      const int r = e / L;
+      const int i = e - r * L;
+      if (r >= rows) continue;
+      const int si = sidx(r, i, pitch, ps);
+      res[si] = cj<T>(mul<T>(res[si], bkf[i]));
+    }
+    __syncthreads();
+    res = fft_rows<T>(res, res == sm ? sm1 : sm, rows, pitch, ps, a.core);
+  }
+
+  // ---------------- store ----------------
+  {
+    const int units = a.nout;
+    const int total = TB * units;
+    const int64_t s = a.st.axis_stride;
+    for (int e = tid; e < total; e += nth) {
+      int r, i;
+      walk(e, a.st.colmap, TB, dTB, units, dOut, r, i);
+      if (r >= rows) continue;
+      const int64_t off = roff_out[r];
+      if constexpr (OP == OP_C2C) {
+        cx<T> v = res[sidx(r, i, pitch, ps)];
+        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
+        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
+      } else if constexpr (OP == OP_C2C_TW) {
+        cx<T> v = res[sidx(r, i, pitch, ps)];
+        const cx<T> w = split_twiddle<T>(reinterpret_cast<const cx<T> *>(a.aux),
+                                         reinterpret_cast<const cx<T> *>(a.aux2), a.aux_s,
+                                         uint32_t(rowaux[r]) * uint32_t(i));
+        v = mul<T>(v, w);
+        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
+        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
+      } else if constexpr (OP == OP_BLUE) {
+        const cx<T> *bk = reinterpret_cast<const cx<T> *>(a.aux);
+        // y = conj(F) * conj(bk) = conj(F * bk)
+        cx<T> v = cj<T>(mul<T>(res[sidx(r, i, pitch, ps)], bk[i]));
+        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
+        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
+      } else if constexpr (OP == OP_R2C_EVEN || OP == OP_R2C_ODD) {
+        cx<T> v = res[sidx(r, i, pitch, ps)];
+        if (OP == OP_R2C_ODD && i == 0) v.y = T(0);
+        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
+        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
+      } else if constexpr (OP == OP_C2R_EVEN) {
+        // x_{2j} = Re F_j, x_{2j+1} = -Im F_j
+        const int j = i >> 1;
+        const cx<T> v = res[sidx(r, j, pitch, ps)];
+        reinterpret_cast<T *>(a.out)[off + i * s] = ((i & 1) ? -v.y : v.x) * fct;
+      } else if constexpr (OP == OP_C2R_ODD) {
+        const cx<T> v = res[sidx(r, i, pitch, ps)];
+        reinterpret_cast<T *>(a.out)[off + i * s] = v.x * fct;
+      }
+    }
+  }
+}
+
+}  // namespace rg

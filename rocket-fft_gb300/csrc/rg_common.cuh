@@ -1,0 +1,102 @@
+// Shared host/device definitions for the GB300 pocketfft transform path.
+//
+// Everything that crosses the host->kernel boundary lives here as plain structs passed by
+// value as kernel parameters (one launch = one "axis job": a batch of 1-D transforms along
+// one axis of a strided array).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rg {
+
+constexpr int kMaxPass = 20;    // radix passes of one on-chip FFT
+constexpr int kMaxBatchDims = 6; // batch (non-transformed) dims after host-side collapsing
+
+// Division by a runtime constant d (1 <= d < 2^31) for unsigned 32-bit numerators via a
+// multiply-high: q = (umulhi(n, m) + n) >> s, the round-up method of Granlund & Montgomery
+// (PLDI'94), with the add done in 64 bits so that no n < 2^32 overflows.
+struct FastDiv {
+  uint32_t d, m, s, pad_;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f{d, 0, 0, 0};
+  uint32_t s = 0;
+  while ((uint64_t(1) << s) < d) ++s;
+  f.s = s;
+  f.m = uint32_t(((uint64_t(1) << 32) * ((uint64_t(1) << s) - d)) / d + 1);
+  return f;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+  uint32_t hi = __umulhi(n, f.m);
+  return uint32_t((uint64_t(hi) + n) >> f.s);
+}
+#endif
+
+// One Stockham radix pass of an on-chip FFT of length L (see rg_fft.cuh).
+struct PassDesc {
+  int R;   // radix
+  int Ns;  // product of the radices of the previous passes
+  int LR;  // L / R butterflies per transform
+  int tw;  // offset of this pass's twiddles in the core table: (R-1)*Ns entries
+  FastDiv dNs, dLR;
+};
+
+// An on-chip FFT of length L as a sequence of radix passes.
+struct FFTCore {
+  int L;
+  int npass;
+  const void *tw;  // complex<T> twiddles, forward sign, all passes back to back
+  PassDesc pass[kMaxPass];
+};
+
+// Global addressing of one side (load or store) of an axis job. Element (row g, position i)
+// lives at  sum_d idx_d(g) * bstride[d] + i * axis_stride  (in units of the side's element
+// type), where idx_d(g) decomposes the row number over bshape with dim 0 fastest.
+struct Side {
+  int64_t axis_stride;
+  int64_t bshape[kMaxBatchDims];
+  int64_t bstride[kMaxBatchDims];
+  int nbd;
+  int colmap;  // 1: consecutive threads walk consecutive rows (rows are adjacent in memory)
+};
+
+// What the kernel does around the on-chip FFT.
+enum Op : int {
+  OP_C2C = 0,        // complex -> complex, length n = L
+  OP_C2C_TW = 1,     // four-step first pass: C2C, then multiply element k of row g by
+                     // W_N^{(g mod aux_n) * k}, N = L * aux_n
+  OP_R2C_EVEN = 2,   // real n = 2L -> n/2+1 complex (half-length complex FFT + split)
+  OP_R2C_ODD = 3,    // real n = L -> n/2+1 complex
+  OP_C2R_EVEN = 4,   // n/2+1 complex -> real n = 2L
+  OP_C2R_ODD = 5,    // n/2+1 complex -> real n = L
+  OP_BLUE = 6,       // complex n -> complex n through a length-L (L >= 2n-1) convolution
+  OP_DCT2 = 7, OP_DCT3 = 8, OP_DCT4_EVEN = 9, OP_DCT1 = 10, OP_DST1 = 11,
+  OP_R2R_FFTPACK_R2H = 12, OP_R2R_FFTPACK_H2R = 13, OP_HARTLEY = 14,
+  OP_COUNT = 15
+};
+
+struct KArgs {
+  const void *in;
+  void *out;
+  Side ld, st;
+  int64_t nrows;   // number of transforms in this launch
+  int TB;          // transforms (rows) per CTA
+  int n;           // logical transform length along the axis
+  int nin, nout;   // elements per row read / written
+  int pitch;       // shared-memory row pitch, in complex elements
+  int ps;          // pad shift: shared index i is stored at i + (i >> ps)
+  int conj_in;     // conjugate while loading (backward transforms run the forward core on
+  int conj_out;    // conjugated data) / while storing
+  int flags;       // op-specific (cosine/ortho/type bits, ...)
+  double fct;      // scale applied to every output
+  const void *aux;   // op-specific table (split twiddles, chirp, ...)
+  const void *aux2;  // op-specific second table (Bluestein spectrum, ...)
+  int aux_n;         // op-specific integer (four-step: number of columns)
+  int aux_s;         // op-specific integer (four-step: low-table split shift)
+  FFTCore core;
+};
+
+}  // namespace rg

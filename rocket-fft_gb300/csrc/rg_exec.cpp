@@ -1,0 +1,593 @@
+// N-d driver: turns a (shape, strides, axes) request into axis jobs and each axis job into
+// one kernel (length fits on chip), a four-step pair (long smooth lengths) or a Bluestein
+// sequence (lengths with a prime factor above 13).
+//
+// Semantics follow the reference's drivers (rocket_fft/_pocketfft_hdronly.h):
+//   c2c      general_nd 3568-3607: axes in the given order, the first reads `in`, later ones
+//            work in place on `out`; fct is applied once (here: by the first axis job).
+//   r2c      3955-3975: r2c along axes.back(), then c2c in place over the other axes.
+//   c2r      3995-4023: c2c over axes[:-1] into a C-contiguous temporary, then c2r along
+//            axes.back() with fct.
+//   c2c_sym  rocket_fft/_pocketfft_numba.cpp:111-143: r2c into the full-size output, then
+//            Hermitian completion (rg_launch.hpp MirrorArgs).
+#include "rg_exec.hpp"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "rg_error.hpp"
+#include "rg_launch.hpp"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------------------
+
+static cudaMemPool_t device_pool() {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    RG_CUDA(cudaMemPoolCreate(&pools[dev], &props));
+    uint64_t thresh = UINT64_MAX;  // keep freed blocks for reuse
+    RG_CUDA(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &thresh));
+  }
+  return pools[dev];
+}
+
+DevBuf::DevBuf(size_t bytes, cudaStream_t st) : st_(st) {
+  if (bytes == 0) bytes = 16;
+  RG_CUDA(cudaMallocFromPoolAsync(&p_, bytes, device_pool(), st));
+}
+
+DevBuf::~DevBuf() {
+  if (p_) cudaFreeAsync(p_, st_);
+}
+
+void pool_trim() { cudaMemPoolTrimTo(device_pool(), 0); }
+
+// ---------------------------------------------------------------------------------------
+// batch geometry
+// ---------------------------------------------------------------------------------------
+
+namespace {
+
+struct Batch {
+  std::vector<int64_t> shape, s_in, s_out;  // fastest first after sorting and merging
+  int64_t nrows = 1;
+};
+
+Batch make_batch(const std::vector<int64_t> &shape, const std::vector<int64_t> &s_in,
+                 const std::vector<int64_t> &s_out, int axis) {
+  struct D {
+    int64_t n, a, b;
+  };
+  std::vector<D> ds;
+  for (int d = 0; d < int(shape.size()); ++d)
+    if (d != axis && shape[d] > 1) ds.push_back({shape[d], s_in[d], s_out[d]});
+  std::stable_sort(ds.begin(), ds.end(), [](const D &x, const D &y) {
+    return std::llabs(x.a) + std::llabs(x.b) < std::llabs(y.a) + std::llabs(y.b);
+  });
+  std::vector<D> m;
+  for (const D &d : ds) {
+    if (!m.empty() && m.back().a * m.back().n == d.a && m.back().b * m.back().n == d.b)
+      m.back().n *= d.n;
+    else
+      m.push_back(d);
+  }
+  Batch b;
+  for (const D &d : m) {
+    b.shape.push_back(d.n);
+    b.s_in.push_back(d.a);
+    b.s_out.push_back(d.b);
+    b.nrows *= d.n;
+  }
+  return b;
+}
+
+Side make_side(int64_t axis_stride, const std::vector<int64_t> &shape,
+               const std::vector<int64_t> &strides) {
+  Side s{};
+  RG_CHECK(shape.size() <= size_t(kMaxBatchDims), RG_ERR_UNSUPPORTED,
+           "too many non-mergeable batch dimensions");
+  s.axis_stride = axis_stride;
+  s.nbd = int(shape.size());
+  for (size_t d = 0; d < shape.size(); ++d) {
+    s.bshape[d] = shape[d];
+    s.bstride[d] = strides[d];
+  }
+  return s;
+}
+
+// prepend a batch dim (fastest) to a side
+Side with_inner(const Side &s, int64_t n, int64_t stride, int64_t new_axis_stride) {
+  RG_CHECK(s.nbd + 1 <= kMaxBatchDims, RG_ERR_UNSUPPORTED, "too many batch dimensions");
+  Side r{};
+  r.axis_stride = new_axis_stride;
+  r.nbd = s.nbd + 1;
+  r.bshape[0] = n;
+  r.bstride[0] = stride;
+  for (int d = 0; d < s.nbd; ++d) {
+    r.bshape[d + 1] = s.bshape[d];
+    r.bstride[d + 1] = s.bstride[d];
+  }
+  return r;
+}
+
+void set_colmap(Side &s) {
+  s.colmap = (s.nbd > 0 && std::llabs(s.bstride[0]) < std::llabs(s.axis_stride)) ? 1 : 0;
+}
+
+Side contiguous_rows(int64_t nrows, int64_t len) {
+  Side s{};
+  s.axis_stride = 1;
+  if (nrows > 1) {
+    s.nbd = 1;
+    s.bshape[0] = nrows;
+    s.bstride[0] = len;
+  }
+  return s;
+}
+
+// Shared-memory geometry of an on-chip job: two ping-pong buffers of TB rows, each row
+// padded (index i stored at i + (i >> ps)) and the row pitch made odd modulo the bank width
+// so that column walks across rows do not conflict.
+int row_pitch(DType dt, int Lsm, int &ps) {
+  const int esz = int(cx_size(dt));
+  ps = dt == DType::F32 ? 4 : 3;
+  int pitch = Lsm + ((Lsm - 1) >> ps) + 1;
+  const int mod = 128 / esz;
+  while (pitch % mod != 1) ++pitch;
+  return pitch;
+}
+
+size_t smem_bytes(DType dt, int TB, int pitch) {
+  return 2 * size_t(TB) * pitch * cx_size(dt) + size_t(TB) * 20 + 16;
+}
+
+bool fits_core(int64_t L, DType dt) {
+  if (L < 1 || L > kMaxCore || !core_smooth(uint64_t(L))) return false;
+  int ps;
+  const int pitch = row_pitch(dt, int(L) + 1, ps);
+  return smem_bytes(dt, 1, pitch) <= max_smem_optin();
+}
+
+struct Geo {
+  int TB, threads, pitch, ps;
+  size_t smem;
+};
+
+// Rows per CTA, threads and shared memory for an on-chip job of core length L whose
+// shared rows need Lsm complex slots.
+Geo choose_geo(DType dt, int L, int Lsm, bool col, int64_t nrows) {
+  Geo g{};
+  g.pitch = row_pitch(dt, Lsm, g.ps);
+  const size_t maxsm = max_smem_optin();
+  int TB;
+  if (col)
+    TB = dt == DType::F32 ? 16 : 8;
+  else
+    TB = std::max(1, (dt == DType::F32 ? 4096 : 2048) / L);
+  if (int64_t(TB) > nrows) TB = int(std::max<int64_t>(1, nrows));
+  const size_t budget_soft = col ? 160 * 1024 : 112 * 1024;
+  for (;;) {
+    const size_t smem = smem_bytes(dt, TB, g.pitch);
+    if (smem <= (TB == 1 ? maxsm : std::min(maxsm, budget_soft))) {
+      const int64_t work = int64_t(TB) * L / (dt == DType::F32 ? 16 : 8);
+      g.TB = TB;
+      g.threads = int(std::min<int64_t>(kMaxThreads, std::max<int64_t>(64, (work + 31) / 32 * 32)));
+      g.smem = smem;
+      return g;
+    }
+    if (TB == 1) throw Error(RG_ERR_INTERNAL, "no launch geometry for length " + std::to_string(L));
+    TB = TB > 4 ? TB - TB / 4 : TB - 1;
+  }
+}
+
+struct Job {
+  DType dt;
+  int op;
+  int n;     // logical length
+  int L;     // core length
+  int Lsm;   // shared slots per row
+  int nin, nout;
+  const void *in;
+  void *out;
+  Side ld, st;
+  int64_t nrows;
+  bool cin, cout;
+  double fct;
+  const void *aux = nullptr, *aux2 = nullptr;
+  int aux_n = 1, aux_s = 0;
+};
+
+void run_job(const Job &j, cudaStream_t st) {
+  if (j.nrows <= 0) return;
+  const CoreTables &ct = get_core(j.L, j.dt);
+  Side ld = j.ld, sd = j.st;
+  set_colmap(ld);
+  set_colmap(sd);
+  const Geo g = choose_geo(j.dt, j.L, j.Lsm, ld.colmap || sd.colmap, j.nrows);
+  KArgs a{};
+  a.in = j.in;
+  a.out = j.out;
+  a.ld = ld;
+  a.st = sd;
+  a.nrows = j.nrows;
+  a.TB = g.TB;
+  a.n = j.n;
+  a.nin = j.nin;
+  a.nout = j.nout;
+  a.pitch = g.pitch;
+  a.ps = g.ps;
+  a.conj_in = j.cin;
+  a.conj_out = j.cout;
+  a.fct = j.fct;
+  a.aux = j.aux;
+  a.aux2 = j.aux2;
+  a.aux_n = j.aux_n;
+  a.aux_s = j.aux_s;
+  a.core = ct.core;
+  LaunchCfg cfg;
+  const int64_t grid = (j.nrows + g.TB - 1) / g.TB;
+  RG_CHECK(grid < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "too many transforms in one call");
+  cfg.grid = unsigned(grid);
+  cfg.threads = g.threads;
+  cfg.smem = g.smem;
+  launch_axis(j.dt, j.op, a, cfg, st);
+}
+
+void pointwise(DType dt, int op, const void *in, const Side &ld, void *out, const Side &sd,
+               int64_t nrows, int nout, int n, bool cin, bool cout, double fct, const void *aux,
+               const void *aux2, cudaStream_t st) {
+  PwArgs p{};
+  p.in = in;
+  p.out = out;
+  p.ld = ld;
+  p.st = sd;
+  p.nrows = nrows;
+  p.nout = nout;
+  p.n = n;
+  p.conj_in = cin;
+  p.conj_out = cout;
+  p.fct = fct;
+  p.aux = aux;
+  p.aux2 = aux2;
+  launch_pointwise(dt, op, p, st);
+}
+
+// Split n = n1 * n2 with both halves on chip, n1 as close to sqrt(n) as possible.
+bool four_step_split(DType dt, int64_t n, int64_t &n1, int64_t &n2) {
+  int64_t best = 0;
+  for (int64_t d = 1; d * d <= n; ++d)
+    if (n % d == 0 && fits_core(d, dt) && fits_core(n / d, dt)) best = d;
+  if (!best) return false;
+  n1 = best;
+  n2 = n / best;
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------
+// complex transforms of a batch of rows (any length)
+// ---------------------------------------------------------------------------------------
+
+void c2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
+              int64_t nrows, bool cin, bool cout, double fct, cudaStream_t st);
+
+void c2c_four_step(DType dt, int64_t n, int64_t n1, int64_t n2, const void *in, const Side &ld,
+                   void *out, const Side &sd, int64_t nrows, bool cin, bool cout, double fct,
+                   cudaStream_t st) {
+  DevBuf ws(size_t(nrows) * size_t(n) * cx_size(dt), st);
+  const SplitTables tw = get_split(uint64_t(n), dt);
+  // pass A: columns j2 of length n1 (stride n2), twiddle W_n^{j2 k1}, into ws[row][k1][j2]
+  Job a{};
+  a.dt = dt;
+  a.op = OP_C2C_TW;
+  a.n = a.L = a.Lsm = a.nin = a.nout = int(n1);
+  a.in = in;
+  a.out = ws.get();
+  a.ld = with_inner(ld, n2, ld.axis_stride, ld.axis_stride * n2);
+  Side wsrows = contiguous_rows(nrows, n);
+  a.st = with_inner(wsrows, n2, 1, n2);
+  a.nrows = nrows * n2;
+  a.cin = cin;
+  a.cout = false;
+  a.fct = 1.0;
+  a.aux = tw.lo;
+  a.aux2 = tw.hi;
+  a.aux_s = tw.shift;
+  a.aux_n = int(n2);
+  run_job(a, st);
+  // pass B: rows k1 of length n2 from ws, output element k2 to out[k2*n1 + k1]
+  Job b{};
+  b.dt = dt;
+  b.op = OP_C2C;
+  b.n = b.L = b.Lsm = b.nin = b.nout = int(n2);
+  b.in = ws.get();
+  b.out = out;
+  b.ld = with_inner(wsrows, n1, n2, 1);
+  b.st = with_inner(sd, n1, sd.axis_stride, sd.axis_stride * n1);
+  b.nrows = nrows * n1;
+  b.cin = false;
+  b.cout = cout;
+  b.fct = fct;
+  run_job(b, st);
+}
+
+void c2c_bluestein_large(DType dt, int64_t n, const void *in, const Side &ld, void *out,
+                         const Side &sd, int64_t nrows, bool cin, bool cout, double fct,
+                         cudaStream_t st) {
+  const BlueTables &bt = get_blue(uint64_t(n), dt);
+  const int64_t m = int64_t(bt.m);
+  DevBuf ws(size_t(nrows) * size_t(m) * cx_size(dt), st);
+  const Side wrows = contiguous_rows(nrows, m);
+  pointwise(dt, PW_BLUE_PRE, in, ld, ws.get(), wrows, nrows, int(m), int(n), cin, false, 1.0, bt.bk,
+            bt.bkf, st);
+  c2c_rows(dt, m, ws.get(), wrows, ws.get(), wrows, nrows, false, false, 1.0, st);
+  pointwise(dt, PW_BLUE_MID, ws.get(), wrows, ws.get(), wrows, nrows, int(m), int(n), false, false,
+            1.0, bt.bk, bt.bkf, st);
+  c2c_rows(dt, m, ws.get(), wrows, ws.get(), wrows, nrows, false, false, 1.0, st);
+  pointwise(dt, PW_BLUE_POST, ws.get(), wrows, out, sd, nrows, int(n), int(n), false, cout, fct,
+            bt.bk, bt.bkf, st);
+}
+
+void c2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
+              int64_t nrows, bool cin, bool cout, double fct, cudaStream_t st) {
+  RG_CHECK(n < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
+  if (fits_core(n, dt)) {
+    Job j{};
+    j.dt = dt;
+    j.op = OP_C2C;
+    j.n = j.L = j.Lsm = j.nin = j.nout = int(n);
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.cin = cin;
+    j.cout = cout;
+    j.fct = fct;
+    run_job(j, st);
+    return;
+  }
+  int64_t n1, n2;
+  if (core_smooth(uint64_t(n)) && four_step_split(dt, n, n1, n2)) {
+    c2c_four_step(dt, n, n1, n2, in, ld, out, sd, nrows, cin, cout, fct, st);
+    return;
+  }
+  RG_CHECK(core_smooth(uint64_t(n)) == false, RG_ERR_UNSUPPORTED,
+           "transform length too large for a two-pass decomposition");
+  const uint64_t m = blue_length(uint64_t(n));
+  if (fits_core(int64_t(m), dt)) {
+    const BlueTables &bt = get_blue(uint64_t(n), dt);
+    Job j{};
+    j.dt = dt;
+    j.op = OP_BLUE;
+    j.n = int(n);
+    j.L = j.Lsm = int(m);
+    j.nin = j.nout = int(n);
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.cin = cin;
+    j.cout = cout;
+    j.fct = fct;
+    j.aux = bt.bk;
+    j.aux2 = bt.bkf;
+    run_job(j, st);
+    return;
+  }
+  c2c_bluestein_large(dt, n, in, ld, out, sd, nrows, cin, cout, fct, st);
+}
+
+// real -> half-complex along rows; conj_out conjugates (reference: forward=false)
+void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
+              int64_t nrows, bool cout, double fct, cudaStream_t st) {
+  RG_CHECK(n < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
+  if (n % 2 == 0 && fits_core(n / 2, dt)) {
+    const int L = int(n / 2);
+    Job j{};
+    j.dt = dt;
+    j.op = OP_R2C_EVEN;
+    j.n = int(n);
+    j.L = L;
+    j.Lsm = L + 1;
+    j.nin = int(n);
+    j.nout = L + 1;
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.cin = false;
+    j.cout = cout;
+    j.fct = fct;
+    j.aux = get_roots(uint64_t(n), uint64_t(L / 2 + 1), dt);
+    run_job(j, st);
+    return;
+  }
+  if (n % 2 == 1 && fits_core(n, dt)) {
+    Job j{};
+    j.dt = dt;
+    j.op = OP_R2C_ODD;
+    j.n = j.L = j.Lsm = j.nin = int(n);
+    j.nout = int(n / 2 + 1);
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.cin = false;
+    j.cout = cout;
+    j.fct = fct;
+    run_job(j, st);
+    return;
+  }
+  // general length: full complex transform of the real row, keep bins 0..n/2
+  DevBuf ws(size_t(nrows) * size_t(n) * cx_size(dt), st);
+  const Side w = contiguous_rows(nrows, n);
+  pointwise(dt, PW_R2C_PACK, in, ld, ws.get(), w, nrows, int(n), int(n), false, false, 1.0, nullptr,
+            nullptr, st);
+  c2c_rows(dt, n, ws.get(), w, ws.get(), w, nrows, false, false, 1.0, st);
+  pointwise(dt, PW_R2C_TAKE, ws.get(), w, out, sd, nrows, int(n / 2 + 1), int(n), false, cout, fct,
+            nullptr, nullptr, st);
+}
+
+// half-complex -> real along rows; conj_in conjugates the input (reference: forward=true)
+void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
+              int64_t nrows, bool cin, double fct, cudaStream_t st) {
+  RG_CHECK(n < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
+  if (n % 2 == 0 && fits_core(n / 2, dt)) {
+    const int L = int(n / 2);
+    Job j{};
+    j.dt = dt;
+    j.op = OP_C2R_EVEN;
+    j.n = int(n);
+    j.L = L;
+    j.Lsm = L + 1;
+    j.nin = L + 1;
+    j.nout = int(n);
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.cin = cin;
+    j.cout = false;
+    j.fct = fct;
+    j.aux = get_roots(uint64_t(n), uint64_t(L / 2 + 1), dt);
+    run_job(j, st);
+    return;
+  }
+  if (n % 2 == 1 && fits_core(n, dt)) {
+    Job j{};
+    j.dt = dt;
+    j.op = OP_C2R_ODD;
+    j.n = j.L = j.Lsm = int(n);
+    j.nin = int(n / 2 + 1);
+    j.nout = int(n);
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.cin = cin;
+    j.cout = false;
+    j.fct = fct;
+    run_job(j, st);
+    return;
+  }
+  DevBuf ws(size_t(nrows) * size_t(n) * cx_size(dt), st);
+  const Side w = contiguous_rows(nrows, n);
+  pointwise(dt, PW_C2R_BUILD, in, ld, ws.get(), w, nrows, int(n), int(n), cin, false, 1.0, nullptr,
+            nullptr, st);
+  c2c_rows(dt, n, ws.get(), w, ws.get(), w, nrows, false, false, 1.0, st);
+  pointwise(dt, PW_C2R_TAKE, ws.get(), w, out, sd, nrows, int(n), int(n), false, false, fct, nullptr,
+            nullptr, st);
+}
+
+bool any_zero(const std::vector<int64_t> &shape) {
+  for (int64_t s : shape)
+    if (s == 0) return true;
+  return false;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// public driver
+// ---------------------------------------------------------------------------------------
+
+void exec_c2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+              double fct, cudaStream_t st) {
+  if (any_zero(out.shape)) return;
+  for (size_t k = 0; k < axes.size(); ++k) {
+    const NdArray &src = k == 0 ? in : out;
+    const int ax = int(axes[k]);
+    const Batch b = make_batch(out.shape, src.stride, out.stride, ax);
+    const Side ld = make_side(src.stride[ax], b.shape, b.s_in);
+    const Side sd = make_side(out.stride[ax], b.shape, b.s_out);
+    c2c_rows(dt, out.shape[ax], src.data, ld, out.data, sd, b.nrows, !forward, !forward,
+             k == 0 ? fct : 1.0, st);
+  }
+}
+
+void exec_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+              double fct, cudaStream_t st) {
+  if (any_zero(in.shape) || axes.empty()) return;
+  const int last = int(axes.back());
+  const Batch b = make_batch(in.shape, in.stride, out.stride, last);
+  const Side ld = make_side(in.stride[last], b.shape, b.s_in);
+  const Side sd = make_side(out.stride[last], b.shape, b.s_out);
+  r2c_rows(dt, in.shape[last], in.data, ld, out.data, sd, b.nrows, !forward, fct, st);
+  if (axes.size() > 1) {
+    NdArray o = out;
+    o.shape = in.shape;
+    o.shape[last] = in.shape[last] / 2 + 1;
+    exec_c2c(dt, o, o, Axes(axes.begin(), axes.end() - 1), forward, 1.0, st);
+  }
+}
+
+void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+              double fct, cudaStream_t st) {
+  if (any_zero(out.shape) || axes.empty()) return;
+  const int last = int(axes.back());
+  std::vector<int64_t> shape_in = out.shape;
+  shape_in[last] = out.shape[last] / 2 + 1;
+  if (axes.size() == 1) {
+    const Batch b = make_batch(out.shape, in.stride, out.stride, last);
+    const Side ld = make_side(in.stride[last], b.shape, b.s_in);
+    const Side sd = make_side(out.stride[last], b.shape, b.s_out);
+    c2r_rows(dt, out.shape[last], in.data, ld, out.data, sd, b.nrows, forward, fct, st);
+    return;
+  }
+  // C-contiguous complex temporary with the input's shape
+  int64_t total = 1;
+  for (int64_t s : shape_in) total *= s;
+  DevBuf tmp(size_t(total) * cx_size(dt), st);
+  NdArray t;
+  t.data = tmp.get();
+  t.shape = shape_in;
+  t.stride.assign(shape_in.size(), 1);
+  for (int d = int(shape_in.size()) - 2; d >= 0; --d) t.stride[d] = t.stride[d + 1] * shape_in[d + 1];
+  NdArray src = in;
+  src.shape = shape_in;
+  exec_c2c(dt, src, t, Axes(axes.begin(), axes.end() - 1), forward, 1.0, st);
+  const Batch b = make_batch(out.shape, t.stride, out.stride, last);
+  const Side ld = make_side(t.stride[last], b.shape, b.s_in);
+  const Side sd = make_side(out.stride[last], b.shape, b.s_out);
+  c2r_rows(dt, out.shape[last], t.data, ld, out.data, sd, b.nrows, forward, fct, st);
+}
+
+void exec_c2c_sym(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+                  double fct, cudaStream_t st) {
+  if (any_zero(in.shape) || axes.empty()) return;
+  exec_r2c(dt, in, out, axes, forward, fct, st);
+  MirrorArgs m{};
+  RG_CHECK(in.shape.size() <= size_t(kMaxDims), RG_ERR_UNSUPPORTED, "too many dimensions");
+  m.data = out.data;
+  m.ndim = int(in.shape.size());
+  m.last = int(axes.back());
+  for (uint64_t a : axes) m.revmask |= 1u << a;
+  m.half = in.shape[m.last] / 2 + 1;
+  m.total = 1;
+  for (int d = 0; d < m.ndim; ++d) {
+    m.shape[d] = in.shape[d];
+    m.stride[d] = out.stride[d];
+    m.total *= d == m.last ? m.half : in.shape[d];
+  }
+  launch_mirror(dt, m, st);
+}
+
+}  // namespace rg

@@ -1,0 +1,47 @@
+// N-d driver of the GB300 pocketfft path: the GPU counterpart of the reference's
+// general_nd / general_r2c / general_c2r and the public c2c/r2c/c2r/dct/dst/r2r_* functions
+// (rocket_fft/_pocketfft_hdronly.h:3568-4091).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "rg_plan.hpp"
+
+namespace rg {
+
+// Strided view of a device array; strides in elements of the array's own type
+// (complex elements for complex arrays, reals for real arrays).
+struct NdArray {
+  void *data = nullptr;
+  std::vector<int64_t> shape, stride;
+};
+
+using Axes = std::vector<uint64_t>;
+
+void exec_c2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+              double fct, cudaStream_t st);
+void exec_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+              double fct, cudaStream_t st);
+void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+              double fct, cudaStream_t st);
+void exec_c2c_sym(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
+                  double fct, cudaStream_t st);
+
+// Device workspace from a per-device stream-ordered pool.
+class DevBuf {
+ public:
+  DevBuf(size_t bytes, cudaStream_t st);
+  ~DevBuf();
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  void *get() const { return p_; }
+
+ private:
+  void *p_ = nullptr;
+  cudaStream_t st_;
+};
+void pool_trim();
+
+}  // namespace rg

@@ -1,0 +1,71 @@
+// Kernel launch layer: typed entry points into the axis-job kernel and the row-wise
+// pointwise kernels, plus a process-wide launch counter.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rg_common.cuh"
+#include "rg_plan.hpp"
+
+namespace rg {
+
+struct LaunchCfg {
+  unsigned grid;
+  int threads;
+  size_t smem;
+};
+
+// Launch axis_kernel<T, op> with the given configuration.
+void launch_axis(DType dt, int op, const KArgs &a, const LaunchCfg &cfg, cudaStream_t st);
+
+// Row-wise elementwise kernels used around multi-kernel transforms. For each row g and
+// output element i (0 <= i < nout) the op reads the input row through `ld` and writes
+// through `st` (both Side descriptors with the row decomposition of the axis kernel).
+enum PwOp : int {
+  PW_BLUE_PRE = 0,   // out[i] = i < n ? conj?(x_i) * conj(bk_i) : 0            (i < m)
+  PW_BLUE_MID = 1,   // out[i] = conj(in_i * bkf_i)                             (i < m)
+  PW_BLUE_POST = 2,  // out[i] = conj?(conj(in_i * bk_i)) * fct                 (i < n)
+  PW_R2C_PACK = 3,   // out[i] = (x_i, 0)                                       (i < n)
+  PW_R2C_TAKE = 4,   // out[i] = conj?(in_i) * fct, imag of bins 0, n/2 zeroed  (i <= n/2)
+  PW_C2R_BUILD = 5,  // out = conj of the Hermitian extension of conj?(X)       (i < n)
+  PW_C2R_TAKE = 6,   // out[i] = Re(in_i) * fct (real output)                   (i < n)
+  PW_COUNT = 7
+};
+
+struct PwArgs {
+  const void *in;
+  void *out;
+  Side ld, st;
+  int64_t nrows;
+  int nout;        // output elements per row
+  int n;           // logical transform length
+  int conj_in, conj_out;
+  double fct;
+  const void *aux, *aux2;
+};
+
+void launch_pointwise(DType dt, int op, const PwArgs &a, cudaStream_t st);
+
+// Hermitian completion for c2c_sym: over every position p of the half-spectrum (last
+// transformed axis cut to n/2+1, C order), q = mirror(p) (i -> (n_i - i) mod n_i on the
+// transformed axes). out[q] = conj(out[p]) when q lies outside the half, or when it lies
+// inside and comes at or after p in C order -- the serial rev_iter loop of the reference's
+// numba_c2c_sym (rocket_fft/_pocketfft_numba.cpp:111-143) leaves exactly this state.
+constexpr int kMaxDims = 16;
+struct MirrorArgs {
+  void *data;
+  int ndim, last;
+  uint32_t revmask;          // bit d set: axis d is transformed
+  int64_t shape[kMaxDims];   // full shape
+  int64_t stride[kMaxDims];  // complex-element strides
+  int64_t half;              // n_last / 2 + 1
+  int64_t total;             // product of the half shape
+};
+void launch_mirror(DType dt, const MirrorArgs &a, cudaStream_t st);
+
+// Largest dynamic shared memory a CTA may use on the current device.
+size_t max_smem_optin();
+
+uint64_t launch_count();
+void note_launch();
+
+}  // namespace rg

@@ -1,0 +1,344 @@
+"""Low-level pocketfft API on the GPU: ``c2c, r2c, c2r, c2c_sym, dct, dst, r2r_fftpack,
+r2r_separable_hartley, r2r_genuine_hartley, good_size``.
+
+Same names, argument order and meaning as the reference's low-level functions
+(``rocket_fft/__init__.py:18-34`` -> ``rocket_fft/pocketfft.py:193-226``):
+
+    c2c(ain, aout, axes, forward, fct, nthreads)
+    r2c / c2r / c2c_sym(ain, aout, axes, forward, fct, nthreads)
+    dct / dst(ain, aout, axes, type, fct, ortho, nthreads)
+    r2r_fftpack(ain, aout, axes, real2hermitian, forward, fct, nthreads)
+    r2r_separable_hartley / r2r_genuine_hartley(ain, aout, axes, fct, nthreads)
+    good_size(n, real) -> int
+
+``aout`` is written in place and nothing is returned, as in the reference. Arrays may be
+NumPy arrays (staged through the GPU), torch tensors (CUDA or CPU) or any object exposing
+``__cuda_array_interface__``. Argument typing follows the reference's Numba intrinsic
+(``rocket_fft/pocketfft.py:147-190``) and its tests (``tests/test_low_level_interface.py:
+200-325``): ``ain``/``aout`` of equal rank, ``axes`` one-dimensional (cast to uint64),
+``forward``/``ortho``/``real2hermitian`` booleans, ``fct`` a float, ``nthreads``/``type``
+integers; violations raise :class:`TypingError`. ``nthreads`` is accepted and ignored.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import numbers
+
+import numpy as np
+
+from . import _lib
+
+__all__ = [
+    "TypingError",
+    "c2c",
+    "r2c",
+    "c2r",
+    "c2c_sym",
+    "dct",
+    "dst",
+    "r2r_fftpack",
+    "r2r_separable_hartley",
+    "r2r_genuine_hartley",
+    "good_size",
+    "set_stream",
+    "plan_cache_entries",
+    "plan_cache_bytes",
+    "plan_cache_clear",
+    "launch_count",
+    "version",
+]
+
+
+class TypingError(TypeError):
+    """Raised for argument types the reference's Numba intrinsics reject at compile time."""
+
+
+RG_OK, RG_ERR_ARG, RG_ERR_UNSUPPORTED, RG_ERR_CUDA, RG_ERR_NOMEM, RG_ERR_INTERNAL = range(6)
+
+try:  # torch is optional for NumPy-only callers
+    import torch as _torch
+except Exception:  # pragma: no cover
+    _torch = None
+
+
+# ---------------------------------------------------------------------------------------
+# argument checks (mirroring the Numba typing of the reference)
+# ---------------------------------------------------------------------------------------
+
+
+def _is_bool(x):
+    return isinstance(x, (bool, np.bool_))
+
+
+def _is_int(x):
+    return isinstance(x, (numbers.Integral, np.integer)) and not _is_bool(x)
+
+
+def _is_float(x):
+    return isinstance(x, (float, np.floating))
+
+
+def _check_bool(x, name):
+    if not _is_bool(x):
+        raise TypingError(f"'{name}' must be a boolean, got {type(x).__name__}")
+    return bool(x)
+
+
+def _check_float(x, name):
+    if not _is_float(x):
+        raise TypingError(f"'{name}' must be a float, got {type(x).__name__}")
+    return float(x)
+
+
+def _check_int(x, name):
+    if not _is_int(x):
+        raise TypingError(f"'{name}' must be an integer, got {type(x).__name__}")
+    return int(x)
+
+
+def _axes_array(axes):
+    if _torch is not None and isinstance(axes, _torch.Tensor):
+        axes = axes.detach().cpu().numpy()
+    if not isinstance(axes, np.ndarray):
+        raise TypingError("'axes' must be an array")
+    if axes.ndim != 1:
+        raise TypingError("Axes must be a one-dimensional array")
+    if not (np.issubdtype(axes.dtype, np.integer) or np.issubdtype(axes.dtype, np.floating)):
+        raise TypingError("'axes' must hold integers")
+    return np.ascontiguousarray(axes.astype(np.uint64))
+
+
+# ---------------------------------------------------------------------------------------
+# array descriptors
+# ---------------------------------------------------------------------------------------
+
+_CAI_ITEMSIZE = {"<f4": 4, "<f8": 8, "<c8": 8, "<c16": 16}
+
+
+class _Arg:
+    """An array argument turned into a numba array struct (kept alive with its owner)."""
+
+    __slots__ = ("struct", "ndim", "itemsize", "kind", "owner", "cuda", "stream")
+
+    def __init__(self, a, name):
+        self.owner = a
+        self.stream = None
+        if isinstance(a, np.ndarray):
+            self._from_parts(a.ctypes.data, a.shape, a.strides, a.itemsize, a.dtype.kind, False)
+        elif _torch is not None and isinstance(a, _torch.Tensor):
+            es = a.element_size()
+            kind = "c" if a.is_complex() else ("f" if a.is_floating_point() else "i")
+            self._from_parts(a.data_ptr(), tuple(a.shape), tuple(s * es for s in a.stride()), es, kind, a.is_cuda)
+            if a.is_cuda:
+                self.stream = _torch.cuda.current_stream(a.device).cuda_stream
+        elif hasattr(a, "__cuda_array_interface__"):
+            cai = a.__cuda_array_interface__
+            typestr = cai["typestr"]
+            if typestr not in _CAI_ITEMSIZE:
+                raise TypingError(f"'{name}': unsupported typestr {typestr}")
+            es = _CAI_ITEMSIZE[typestr]
+            shape = tuple(cai["shape"])
+            strides = cai.get("strides")
+            if strides is None:
+                strides, acc = [], es
+                for s in reversed(shape):
+                    strides.insert(0, acc)
+                    acc *= s
+            self._from_parts(cai["data"][0], shape, tuple(strides), es, typestr[1], True)
+            st = cai.get("stream")
+            if isinstance(st, int) and st > 2:
+                self.stream = st
+        else:
+            raise TypingError(f"'{name}' must be an array, got {type(a).__name__}")
+
+    def _from_parts(self, ptr, shape, strides, itemsize, kind, cuda):
+        ndim = len(shape)
+        st = _lib.struct_type(ndim)()
+        st.meminfo = None
+        st.parent = None
+        st.nitems = int(np.prod(shape)) if ndim else 1
+        st.itemsize = itemsize
+        st.data = ptr
+        for i in range(ndim):
+            st.shape_and_strides[i] = int(shape[i])
+            st.shape_and_strides[ndim + i] = int(strides[i])
+        self.struct = st
+        self.ndim = ndim
+        self.itemsize = itemsize
+        self.kind = kind
+        self.cuda = cuda
+
+
+def _axes_struct(ax):
+    st = _lib.struct_type(1)()
+    st.nitems = ax.size
+    st.itemsize = 8
+    st.data = ax.ctypes.data
+    st.shape_and_strides[0] = ax.size
+    st.shape_and_strides[1] = 8
+    return st
+
+
+def _raise_status(code, fname):
+    if code == RG_OK:
+        return
+    msg = f"{fname}: {_lib.last_error()}"
+    if code == RG_ERR_ARG:
+        raise ValueError(msg)
+    if code == RG_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if code == RG_ERR_NOMEM:
+        raise MemoryError(msg)
+    raise RuntimeError(msg)
+
+
+def _prepare(ain, aout, axes):
+    a = _Arg(ain, "ain")
+    b = _Arg(aout, "aout")
+    if a.ndim != b.ndim:
+        raise TypingError("Input and output array must have the same number of dimensions")
+    ax = _axes_array(axes)
+    return a, b, ax
+
+
+def _call(fname, a, b, ax, *rest):
+    lib = _lib.load()
+    stream = a.stream or b.stream
+    if stream is not None:
+        lib.rocketgpu_set_stream(ctypes.c_void_p(stream))
+    else:
+        lib.rocketgpu_set_stream(None)
+    axs = _axes_struct(ax)
+    fn = getattr(lib, fname)
+    code = fn(a.ndim, ctypes.byref(a.struct), ctypes.byref(b.struct), ctypes.byref(axs), *rest)
+    _raise_status(code, fname[:-3])
+
+
+# ---------------------------------------------------------------------------------------
+# public low-level API
+# ---------------------------------------------------------------------------------------
+
+
+def _cmplx_call(fname, ain, aout, axes, forward, fct, nthreads):
+    a, b, ax = _prepare(ain, aout, axes)
+    forward = _check_bool(forward, "forward")
+    fct = _check_float(fct, "fct")
+    nthreads = _check_int(nthreads, "nthreads")
+    _call(fname, a, b, ax, forward, fct, max(nthreads, 0))
+
+
+def c2c(ain, aout, axes, forward, fct, nthreads):
+    """Complex-to-complex FFT over ``axes`` (``rocket_fft/_pocketfft_numba.cpp:31-49``)."""
+    _cmplx_call("numba_c2c_st", ain, aout, axes, forward, fct, nthreads)
+
+
+def r2c(ain, aout, axes, forward, fct, nthreads):
+    """Real-to-half-complex FFT; last axis of ``aout`` is ``n//2+1``
+    (``rocket_fft/_pocketfft_numba.cpp:91-109``)."""
+    _cmplx_call("numba_r2c_st", ain, aout, axes, forward, fct, nthreads)
+
+
+def c2r(ain, aout, axes, forward, fct, nthreads):
+    """Half-complex-to-real FFT; ``aout`` carries the real shape
+    (``rocket_fft/_pocketfft_numba.cpp:145-163``)."""
+    _cmplx_call("numba_c2r_st", ain, aout, axes, forward, fct, nthreads)
+
+
+def c2c_sym(ain, aout, axes, forward, fct, nthreads):
+    """Real-input FFT into a full-size complex output completed by Hermitian symmetry
+    (``rocket_fft/_pocketfft_numba.cpp:111-143``)."""
+    _cmplx_call("numba_c2c_sym_st", ain, aout, axes, forward, fct, nthreads)
+
+
+def _real_call(fname, ain, aout, axes, type, fct, ortho, nthreads):
+    a, b, ax = _prepare(ain, aout, axes)
+    type = _check_int(type, "type")
+    fct = _check_float(fct, "fct")
+    ortho = _check_bool(ortho, "ortho")
+    nthreads = _check_int(nthreads, "nthreads")
+    if type < 0:
+        raise ValueError("invalid DCT/DST type")
+    _call(fname, a, b, ax, type, fct, ortho, max(nthreads, 0))
+
+
+def dct(ain, aout, axes, type, fct, ortho, nthreads):
+    """Discrete cosine transform of type 1-4 (``rocket_fft/_pocketfft_numba.cpp:51-69``)."""
+    _real_call("numba_dct_st", ain, aout, axes, type, fct, ortho, nthreads)
+
+
+def dst(ain, aout, axes, type, fct, ortho, nthreads):
+    """Discrete sine transform of type 1-4 (``rocket_fft/_pocketfft_numba.cpp:71-89``)."""
+    _real_call("numba_dst_st", ain, aout, axes, type, fct, ortho, nthreads)
+
+
+def r2r_fftpack(ain, aout, axes, real2hermitian, forward, fct, nthreads):
+    """FFTPACK-layout real transform (``rocket_fft/_pocketfft_numba.cpp:165-183``)."""
+    a, b, ax = _prepare(ain, aout, axes)
+    real2hermitian = _check_bool(real2hermitian, "real2hermitian")
+    forward = _check_bool(forward, "forward")
+    fct = _check_float(fct, "fct")
+    nthreads = _check_int(nthreads, "nthreads")
+    _call("numba_r2r_fftpack_st", a, b, ax, real2hermitian, forward, fct, max(nthreads, 0))
+
+
+def _hartley_call(fname, ain, aout, axes, fct, nthreads):
+    a, b, ax = _prepare(ain, aout, axes)
+    fct = _check_float(fct, "fct")
+    nthreads = _check_int(nthreads, "nthreads")
+    _call(fname, a, b, ax, fct, max(nthreads, 0))
+
+
+def r2r_separable_hartley(ain, aout, axes, fct, nthreads):
+    """Separable Hartley transform (``rocket_fft/_pocketfft_numba.cpp:185-203``)."""
+    _hartley_call("numba_r2r_separable_hartley_st", ain, aout, axes, fct, nthreads)
+
+
+def r2r_genuine_hartley(ain, aout, axes, fct, nthreads):
+    """Genuine (non-separable) Hartley transform (``rocket_fft/_pocketfft_numba.cpp:205-223``)."""
+    _hartley_call("numba_r2r_genuine_hartley_st", ain, aout, axes, fct, nthreads)
+
+
+def good_size(n, real):
+    """Smallest fast length >= n: 2,3,5,7,11-smooth (``real=False``) or 2,3,5-smooth
+    (``real=True``); ``rocket_fft/_pocketfft_numba.cpp:25-29``."""
+    if not (_is_int(n) or _is_bool(n)):
+        raise TypingError("The first argument 'n' must be an integer")
+    if not (_is_int(real) or _is_bool(real)):
+        raise TypingError("The second argument 'real' must be a boolean")
+    n = int(n) & 0xFFFFFFFFFFFFFFFF  # zero-extended to u64 like the intrinsic
+    return int(_lib.load().numba_good_size(n, bool(int(real) & 1)))
+
+
+# ---------------------------------------------------------------------------------------
+# runtime control
+# ---------------------------------------------------------------------------------------
+
+
+def set_stream(stream):
+    """Issue this thread's later transforms on ``stream`` (a ``torch.cuda.Stream``, a raw
+    ``cudaStream_t`` integer, or ``None`` for the legacy default stream)."""
+    if stream is not None and not isinstance(stream, int):
+        stream = stream.cuda_stream
+    _lib.load().rocketgpu_set_stream(ctypes.c_void_p(stream) if stream else None)
+
+
+def plan_cache_entries():
+    return int(_lib.load().rocketgpu_plan_cache_entries())
+
+
+def plan_cache_bytes():
+    return int(_lib.load().rocketgpu_plan_cache_bytes())
+
+
+def plan_cache_clear():
+    _raise_status(_lib.load().rocketgpu_plan_cache_clear(), "plan_cache_clear")
+
+
+def launch_count():
+    """Kernel launches issued by the library since it was loaded."""
+    return int(_lib.load().rocketgpu_launch_count())
+
+
+def version():
+    return _lib.load().rocketgpu_version().decode()

@@ -1,0 +1,30 @@
+"""Host-compiled checks of device arithmetic (no GPU needed): the radix butterflies of the
+on-chip FFT against a naive long-double DFT."""
+
+from __future__ import annotations
+
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from conftest import PKG_DIR, ROOT
+
+HERE = Path(__file__).resolve().parent
+
+
+def _nvcc():
+    for cand in ("/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and Path(cand).exists():
+            return cand
+    pytest.skip("nvcc not available")
+
+
+def test_butterflies(tmp_path):
+    exe = tmp_path / "butterflies"
+    subprocess.run([_nvcc(), "-O2", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
+                    f"-I{ROOT / 'include'}", str(HERE / "native" / "butterflies.cu"), "-o", str(exe)],
+                   check=True, capture_output=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

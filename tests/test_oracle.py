@@ -1,0 +1,118 @@
+"""Pin the oracle port (oracle/pocketfft_port.cpp) to the reference.
+
+* against the golden vectors the reference itself produced (tests/golden), everywhere;
+* against the reference compiled in place (oracle/_ref) on random inputs for every transform
+  family, where that build exists;
+* against FFTW's DCT/DST reference data shipped with SciPy (scipy/fftpack/tests/
+  fftw_*_ref.npz), the golden data the reference's own test suite loads
+  (tests/test_scipy_testsuite.py:1199-1246, 1432-1442), where SciPy ships it.
+"""
+
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+
+TOL = {"f32": 1e-6, "f64": 1e-13}
+RDT = {"f32": np.float32, "f64": np.float64}
+
+
+@pytest.fixture(scope="module")
+def P():
+    return oracle.port()
+
+
+def test_port_matches_golden(P, golden):
+    data, meta = golden
+    bad = []
+    for i, c in enumerate(meta):
+        x, want = data[f"in_{i}"], data[f"out_{i}"]
+        got = np.empty_like(want)
+        getattr(P, c["kind"])(x.copy(), got, c["axes"], c["forward"], c["fct"])
+        e = oracle.rel_l2(got, want)
+        if not e <= TOL[c["prec"]]:
+            bad.append((i, c, e))
+    assert not bad, bad[:5]
+
+
+def test_port_good_size(P, golden):
+    data, _ = golden
+    ns = data["gs_n"]
+    assert all(P.good_size(int(n), False) == int(g) for n, g in zip(ns, data["gs_cmplx"]))
+    assert all(P.good_size(int(n), True) == int(g) for n, g in zip(ns, data["gs_real"]))
+
+
+SHAPES = [((17,), [0]), ((16,), [0]), ((9, 8), [0, 1]), ((3, 10, 7), [2, 0]), ((64,), [0]),
+          ((31,), [0]), ((2,), [0]), ((100,), [0]), ((4099,), [0]), ((5, 6), [1, 1])]
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference oracle not built on this host")
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("shape,axes", SHAPES)
+def test_port_matches_reference_real_transforms(P, prec, shape, axes):
+    R = oracle.ref()
+    rng = np.random.default_rng(hash((prec, shape)) & 0xFFFF)
+    x = rng.standard_normal(shape).astype(RDT[prec])
+    tol = TOL[prec]
+    for kind in ("dct", "dst"):
+        for t in (1, 2, 3, 4):
+            if kind == "dct" and t == 1 and any(shape[a] == 1 for a in axes):
+                continue
+            for ortho in (False, True):
+                a, b = np.empty_like(x), np.empty_like(x)
+                getattr(P, kind)(x, a, axes, t, 0.5, ortho)
+                getattr(R, kind)(x, b, axes, t, 0.5, ortho)
+                assert oracle.rel_l2(a, b) <= tol, (kind, t, ortho)
+    for r2h in (True, False):
+        for fw in (True, False):
+            a, b = np.empty_like(x), np.empty_like(x)
+            P.r2r_fftpack(x, a, axes, r2h, fw, 1.0)
+            R.r2r_fftpack(x, b, axes, r2h, fw, 1.0)
+            assert oracle.rel_l2(a, b) <= tol, ("fftpack", r2h, fw)
+    for k in ("r2r_separable_hartley", "r2r_genuine_hartley"):
+        a, b = np.empty_like(x), np.empty_like(x)
+        getattr(P, k)(x, a, axes, 1.0)
+        getattr(R, k)(x, b, axes, 1.0)
+        assert oracle.rel_l2(a, b) <= tol, k
+
+
+def test_dct1_length1_is_an_error(P):
+    """The reference's DCT-I plan needs a length-2(n-1) FFT: n = 1 raises (HDR:2926)."""
+    x = np.ones(1)
+    with pytest.raises(oracle.OracleError):
+        P.dct(x, np.empty_like(x), [0], 1, 1.0, False)
+
+
+def _fftw_dir():
+    try:
+        import scipy
+    except ImportError:
+        return None
+    d = Path(scipy.__file__).parent / "fftpack" / "tests"
+    return d if (d / "fftw_double_ref.npz").exists() else None
+
+
+@pytest.mark.skipif(_fftw_dir() is None, reason="SciPy's FFTW reference data not installed")
+@pytest.mark.parametrize("prec,fname", [("f64", "fftw_double_ref.npz"), ("f32", "fftw_single_ref.npz")])
+def test_port_against_fftw_dct_dst(P, prec, fname):
+    """FFTW's unnormalised DCT/DST I-IV of x = arange(n) (the data the reference's SciPy
+    test-suite port compares against)."""
+    data = np.load(_fftw_dir() / fname)
+    checked = 0
+    for key in data.files:
+        parts = key.split("_")  # e.g. dct_2_16
+        if len(parts) != 3 or parts[0] not in ("dct", "dst"):
+            continue
+        kind, t, n = parts[0], int(parts[1]), int(parts[2])
+        x = np.arange(n, dtype=RDT[prec])
+        y = np.empty_like(x)
+        getattr(P, kind)(x, y, [0], t, 1.0, False)
+        want = data[key]
+        e = oracle.rel_l2(y, want)
+        assert e <= (1e-5 if prec == "f32" else 1e-12), (key, e)
+        checked += 1
+    assert checked > 0
