@@ -1,0 +1,319 @@
+"""Benchmark of the pocketfft transform path on GB300.
+
+Workload (one step): 3-D real-to-complex FFT of a 256^3 float32 volume iid U(-1,1) over axes
+[0, 1, 2] with fct = 1, then the complex-to-real inverse with fct = 1/256^3 -- the 3-D round
+trip of rocket-fft's low-level r2c/c2r. A step is two transforms; `value` is transforms/s of
+the whole job (all GPUs), with inputs resident in device memory; `e2e` is the same metric
+through the C ABI with host (pinned) buffers, host<->device copies inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's CPU algorithm (the oracle restatement of
+rocket-fft's pocketfft, oracle/pocketfft_port.cpp, all host threads) on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 256
+SHAPE = (N, N, N)
+HALF = (N, N, N // 2 + 1)
+AXES = np.array([0, 1, 2], dtype=np.int64)
+FCT_INV = 1.0 / N**3
+# algorithmic bytes: one read of the input and one write of the output per transform
+BYTES_R2C = N**3 * 4 + N * N * (N // 2 + 1) * 8
+BYTES_STEP = 2 * BYTES_R2C
+ROTATE = 4  # distinct volumes cycled through so that every step starts from cold L2
+METRIC = "transforms/s"
+WORKLOAD = "3-D r2c + c2r round trip, float32 256x256x256, axes [0,1,2], fct 1 and 1/256^3"
+
+# DRAM traffic per launch (read + write bytes) of the dominant kernel from an ncu capture of
+# this workload, see profiles/axis_c2c_f32_256cube.md; None until captured.
+NCU_TRAFFIC = {}
+
+
+def load_package():
+    name = "rocket_fft_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    pkg = ROOT / "rocket-fft_gb300"
+    spec = importlib.util.spec_from_file_location(name, pkg / "__init__.py", submodule_search_locations=[str(pkg)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"rg_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(r[0] for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_round_trip_rate(P, nthreads, reps, rng):
+    """Transforms/s of the oracle port on the host: `reps` round trips of the 256^3 volume."""
+    x = rng.uniform(-1, 1, SHAPE).astype(np.float32)
+    X = np.empty(HALF, np.complex64)
+    y = np.empty(SHAPE, np.float32)
+    P.r2c(x, X, [0, 1, 2], True, 1.0, nthreads)  # plans warm
+    P.c2r(X, y, [0, 1, 2], False, FCT_INV, nthreads)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        P.r2c(x, X, [0, 1, 2], True, 1.0, nthreads)
+        P.c2r(X, y, [0, 1, 2], False, FCT_INV, nthreads)
+    dt = time.perf_counter() - t0
+    return 2 * reps / dt, dt
+
+
+def run_reference(args):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    import oracle
+
+    P = oracle.port()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, SHAPE).astype(np.float32)
+    X = np.empty(HALF, np.complex64)
+    y = np.empty(SHAPE, np.float32)
+    for _ in range(args.warmup):
+        P.r2c(x, X, [0, 1, 2], True, 1.0, cores)
+        P.c2r(X, y, [0, 1, 2], False, FCT_INV, cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        P.r2c(x, X, [0, 1, 2], True, 1.0, cores)
+        P.c2r(X, y, [0, 1, 2], False, FCT_INV, cores)
+    dt = time.perf_counter() - t0
+    value = 2 * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "transforms/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "global_batch": 1, "l2": "cpu"},
+        "cpu_baseline": {"value": value, "unit": "transforms/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} round trips of the full 256^3 volume, nthreads={cores}"},
+        "e2e": {"value": value, "unit": "transforms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rg = load_package()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+    xs = [torch.rand(SHAPE, device=dev, generator=gen) * 2 - 1 for _ in range(ROTATE)]
+    Xs = [torch.empty(HALF, dtype=torch.complex64, device=dev) for _ in range(ROTATE)]
+    ys = [torch.empty(SHAPE, dtype=torch.float32, device=dev) for _ in range(ROTATE)]
+    stream = torch.cuda.current_stream(dev)
+
+    def step(i):
+        k = i % ROTATE
+        rg.r2c(xs[k], Xs[k], AXES, True, 1.0, 1)
+        rg.c2r(Xs[k], ys[k], AXES, False, FCT_INV, 1)
+
+    for i in range(args.warmup):
+        step(i)
+    barrier()
+    launches0 = rg.launch_count()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        start.record(stream)
+        for i in range(args.steps):
+            step(i)
+        stop.record(stream)
+        barrier()
+    launches = rg.launch_count() - launches0
+    ms = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 2 * args.steps / (ms / 1e3)
+
+    # accuracy of one step against the FP64 oracle (host, this rank's first volume)
+    acc = {}
+    if rank == 0:
+        import oracle
+
+        x0 = xs[0].cpu().numpy()
+        step(0)
+        torch.cuda.synchronize()
+        want = np.empty(HALF, np.complex128)
+        oracle.port().r2c(x0.astype(np.float64), want, [0, 1, 2], True, 1.0, os.cpu_count() or 1)
+        acc["r2c_rel_l2_vs_fp64"] = oracle.rel_l2(Xs[0].cpu().numpy(), want)
+        acc["round_trip_rel_l2"] = oracle.rel_l2(ys[0].cpu().numpy(), x0)
+
+    # per-kernel profile over the same steps (events around every launch; separate pass)
+    rg.profile_reset()
+    rg.profile_enable(True)
+    for i in range(args.steps):
+        step(i)
+    stats = rg.profile_read()
+    rg.profile_enable(False)
+    total_ms = sum(s["total_ms"] for s in stats) or 1.0
+    dom = max(stats, key=lambda s: s["total_ms"])
+    achieved = dom["bytes"] / dom["launches"] / (dom["total_ms"] / dom["launches"] / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = NCU_TRAFFIC.get(dom["name"])
+
+    # e2e: the same round trip through the C ABI on pinned host arrays
+    e2e = None
+    if rank == 0:
+        hx = torch.empty(SHAPE, dtype=torch.float32, pin_memory=True)
+        hx.copy_(xs[0].cpu())
+        hX = torch.empty(HALF, dtype=torch.complex64, pin_memory=True)
+        hy = torch.empty(SHAPE, dtype=torch.float32, pin_memory=True)
+        nx, nX, ny = hx.numpy(), hX.numpy(), hy.numpy()
+        rg.set_stream(None)
+        for _ in range(2):
+            rg.r2c(nx, nX, AXES, True, 1.0, 1)
+            rg.c2r(nX, ny, AXES, False, FCT_INV, 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rg.r2c(nx, nX, AXES, True, 1.0, 1)
+            rg.c2r(nX, ny, AXES, False, FCT_INV, 1)
+        dt = time.perf_counter() - t0
+        e2e = {"value": 2 * args.steps / dt, "unit": "transforms/s",
+               "h2d_bytes_per_step": int(nx.nbytes + nX.nbytes), "d2h_bytes_per_step": int(nX.nbytes + ny.nbytes),
+               "path": "numba_r2c/numba_c2r C ABI, host pinned numpy arrays staged by the library"}
+
+    # CPU baseline: bounded sample of the same workload on the host (rank 0 only)
+    cpu = None
+    if rank == 0 and world == 1:
+        import oracle
+
+        cores = os.cpu_count() or 1
+        rate, dt = cpu_round_trip_rate(oracle.port(), cores, 2, np.random.default_rng(0))
+        cpu = {"value": rate, "unit": "transforms/s", "cores": cores, "kind": "port",
+               "sample": f"2 round trips of the full 256^3 volume ({dt:.2f} s), nthreads={cores}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "transforms/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded U(-1,1) volumes)",
+            "config": {"workload": WORKLOAD, "global_batch": world, "rotating_volumes": ROTATE,
+                       "l2": f"inputs rotate over {ROTATE} volumes ({ROTATE * (BYTES_STEP // 2) / 1e6:.0f} MB) > L2",
+                       "step_bytes": BYTES_STEP, "step_gbs": BYTES_STEP / (ms / args.steps / 1e3) / 1e9,
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "launch_ms": dom["total_ms"] / dom["launches"],
+                         "bytes_per_launch": dom["bytes"] // dom["launches"],
+                         "share": dom["total_ms"] / total_ms},
+            "kernels": [{"name": s["name"], "launches": s["launches"], "ms": s["total_ms"],
+                         "share": s["total_ms"] / total_ms,
+                         "gbs": s["bytes"] / (s["total_ms"] / 1e3) / 1e9 if s["total_ms"] else None} for s in stats],
+            "accuracy": acc,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -132,6 +132,21 @@ int rocketgpu_plan_cache_clear(void);
 /* Kernel launches issued by this library since load (all threads). */
 uint64_t rocketgpu_launch_count(void);
 
+/* Event-based per-kernel profile. While enabled, every kernel launch is bracketed by CUDA
+ * events on its stream; rocketgpu_profile_read synchronises them and returns per-kernel-name
+ * aggregates (launches, summed device milliseconds, summed algorithmic bytes = one read of the
+ * launch's input rows plus one write of its output rows). Returns the number of entries
+ * written (at most max). */
+typedef struct rocketgpu_kstat {
+  char name[48];
+  uint64_t launches;
+  double total_ms;
+  uint64_t bytes;
+} rocketgpu_kstat_t;
+void rocketgpu_profile_enable(int on);
+int rocketgpu_profile_read(rocketgpu_kstat_t *out, int max);
+void rocketgpu_profile_reset(void);
+
 /* Library version string. */
 const char *rocketgpu_version(void);
 

@@ -19,6 +19,9 @@ from .pocketfft import (  # noqa: F401
     plan_cache_bytes,
     plan_cache_clear,
     plan_cache_entries,
+    profile_enable,
+    profile_read,
+    profile_reset,
     r2c,
     r2r_fftpack,
     r2r_genuine_hartley,

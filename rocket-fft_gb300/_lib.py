@@ -31,6 +31,13 @@ class ArrayStructBase(ctypes.Structure):
     ]
 
 
+class KStat(ctypes.Structure):
+    """rocketgpu_kstat_t"""
+
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_uint64), ("total_ms", ctypes.c_double),
+                ("bytes", ctypes.c_uint64)]
+
+
 _struct_types: dict[int, type] = {}
 
 
@@ -75,6 +82,11 @@ def _declare(lib):
     lib.rocketgpu_plan_cache_clear.restype = i32
     lib.rocketgpu_launch_count.restype = u64
     lib.rocketgpu_version.restype = ctypes.c_char_p
+    lib.rocketgpu_profile_enable.argtypes = [ctypes.c_int]
+    lib.rocketgpu_profile_enable.restype = None
+    lib.rocketgpu_profile_read.argtypes = [ctypes.POINTER(KStat), ctypes.c_int]
+    lib.rocketgpu_profile_read.restype = i32
+    lib.rocketgpu_profile_reset.restype = None
     return lib
 
 

@@ -396,4 +396,26 @@ RG_EXPORT int rocketgpu_plan_cache_clear(void) {
 
 RG_EXPORT uint64_t rocketgpu_launch_count(void) { return rg::launch_count(); }
 
+RG_EXPORT void rocketgpu_profile_enable(int on) { rg::profile_enable(on != 0); }
+
+RG_EXPORT int rocketgpu_profile_read(rocketgpu_kstat_t *out, int max) {
+  int n = 0;
+  guarded([&] {
+    const auto stats = rg::profile_read();
+    for (const auto &k : stats) {
+      if (n >= max) break;
+      std::memcpy(out[n].name, k.name, sizeof(out[n].name));
+      out[n].launches = k.launches;
+      out[n].total_ms = k.total_ms;
+      out[n].bytes = k.bytes;
+      ++n;
+    }
+  });
+  return n;
+}
+
+RG_EXPORT void rocketgpu_profile_reset(void) {
+  guarded([] { rg::profile_reset(); });
+}
+
 RG_EXPORT const char *rocketgpu_version(void) { return "rocket-fft_gb300 0.1.0 (sm_103a)"; }

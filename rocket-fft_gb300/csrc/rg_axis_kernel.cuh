@@ -50,6 +50,22 @@ __device__ __forceinline__ cx<T> split_twiddle(const cx<T> *__restrict__ lo, con
   return mul<T>(a, b);
 }
 
+// One input unit of an op: a complex element, or for the even-length real transforms the
+// real pair (x_2i, x_2i+1) read as one 8/16-byte access when the row is contiguous and aligned.
+template <typename T, int OP>
+__device__ __forceinline__ cx<T> load_unit(const void *base, int64_t off, int i, int64_t s) {
+  if constexpr (OP == OP_R2C_EVEN) {
+    const T *in = reinterpret_cast<const T *>(base);
+    if (s == 1 && (reinterpret_cast<uintptr_t>(in + off) & (sizeof(cx<T>) - 1)) == 0)
+      return __ldg(reinterpret_cast<const cx<T> *>(in + off) + i);
+    return mk<T>(__ldg(in + off + 2 * i * s), __ldg(in + off + (2 * i + 1) * s));
+  } else if constexpr (OP == OP_R2C_ODD) {
+    return mk<T>(__ldg(reinterpret_cast<const T *>(base) + off + i * s), T(0));
+  } else {
+    return __ldg(reinterpret_cast<const cx<T> *>(base) + off + i * s);
+  }
+}
+
 template <typename T, int OP>
 __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs a, FastDiv dTB,
                                                    FastDiv dIn, FastDiv dOut) {
@@ -78,55 +94,59 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
   const int L = a.core.L;
 
   // ---------------- load ----------------
+  // Each thread gathers kBatch independent elements into registers before writing any of
+  // them to shared memory, so that kBatch global loads are in flight per thread.
   {
+    constexpr int kBatch = 8;
     const int units = a.nin;
     const int total = TB * units;
     const int64_t s = a.ld.axis_stride;
-    for (int e = tid; e < total; e += nth) {
-      int r, i;
-      walk(e, a.ld.colmap, TB, dTB, units, dIn, r, i);
-      if (r >= rows) continue;
-      const int64_t off = roff_in[r];
-      if constexpr (OP == OP_C2C || OP == OP_C2C_TW) {
-        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
-        cx<T> v = in[off + i * s];
-        if (cin) v.y = -v.y;
-        sm[sidx(r, i, pitch, ps)] = v;
-      } else if constexpr (OP == OP_BLUE) {
-        // a_j = x_j * conj(bk_j), zero-padded to L below
-        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
-        const cx<T> *bk = reinterpret_cast<const cx<T> *>(a.aux);
-        cx<T> v = in[off + i * s];
-        if (cin) v.y = -v.y;
-        sm[sidx(r, i, pitch, ps)] = mulc<T>(v, bk[i]);
-      } else if constexpr (OP == OP_R2C_EVEN) {
-        // units = n real values; pair 2j, 2j+1 becomes complex element j
-        const T *in = reinterpret_cast<const T *>(a.in);
-        const T v = in[off + i * s];
-        T *sr = reinterpret_cast<T *>(sm + r * pitch);
-        const int j = i >> 1;
-        sr[2 * (j + (j >> ps)) + (i & 1)] = v;
-      } else if constexpr (OP == OP_R2C_ODD) {
-        const T *in = reinterpret_cast<const T *>(a.in);
-        sm[sidx(r, i, pitch, ps)] = mk<T>(in[off + i * s], T(0));
-      } else if constexpr (OP == OP_C2R_EVEN) {
-        // units = L+1 Hermitian bins; imaginary parts of bins 0 and L are ignored
-        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
-        cx<T> v = in[off + i * s];
-        if (cin) v.y = -v.y;
-        if (i == 0 || i == L) v.y = T(0);
-        sm[sidx(r, i, pitch, ps)] = v;
-      } else if constexpr (OP == OP_C2R_ODD) {
-        // units = (n+1)/2 bins; build conj of the full Hermitian spectrum:
-        //   W_0 = Re X_0, W_i = conj(X_i), W_{n-i} = X_i
-        const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
-        cx<T> v = in[off + i * s];
-        if (cin) v.y = -v.y;
-        if (i == 0) {
-          sm[sidx(r, 0, pitch, ps)] = mk<T>(v.x, T(0));
-        } else {
-          sm[sidx(r, i, pitch, ps)] = cj<T>(v);
-          sm[sidx(r, L - i, pitch, ps)] = v;
+    for (int e0 = tid; e0 < total; e0 += nth * kBatch) {
+      cx<T> v[kBatch];
+      int rr[kBatch], ii[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * nth;
+        rr[u] = -1;
+        if (e < total) {
+          int r, i;
+          walk(e, a.ld.colmap, TB, dTB, units, dIn, r, i);
+          if (r < rows) {
+            rr[u] = r;
+            ii[u] = i;
+            v[u] = load_unit<T, OP>(a.in, roff_in[r], i, s);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        if (rr[u] < 0) continue;
+        const int r = rr[u], i = ii[u];
+        cx<T> x = v[u];
+        if constexpr (OP == OP_C2C || OP == OP_C2C_TW) {
+          if (cin) x.y = -x.y;
+          sm[sidx(r, i, pitch, ps)] = x;
+        } else if constexpr (OP == OP_BLUE) {
+          // a_j = x_j * conj(bk_j), zero-padded to L below
+          if (cin) x.y = -x.y;
+          sm[sidx(r, i, pitch, ps)] = mulc<T>(x, reinterpret_cast<const cx<T> *>(a.aux)[i]);
+        } else if constexpr (OP == OP_R2C_EVEN || OP == OP_R2C_ODD) {
+          sm[sidx(r, i, pitch, ps)] = x;  // (x_2j, x_2j+1) or (x_j, 0)
+        } else if constexpr (OP == OP_C2R_EVEN) {
+          // units = L+1 Hermitian bins; imaginary parts of bins 0 and L are ignored
+          if (cin) x.y = -x.y;
+          if (i == 0 || i == L) x.y = T(0);
+          sm[sidx(r, i, pitch, ps)] = x;
+        } else if constexpr (OP == OP_C2R_ODD) {
+          // units = (n+1)/2 bins; build conj of the full Hermitian spectrum:
+          //   W_0 = Re X_0, W_i = conj(X_i), W_{n-i} = X_i
+          if (cin) x.y = -x.y;
+          if (i == 0) {
+            sm[sidx(r, 0, pitch, ps)] = mk<T>(x.x, T(0));
+          } else {
+            sm[sidx(r, i, pitch, ps)] = cj<T>(x);
+            sm[sidx(r, L - i, pitch, ps)] = x;
+          }
         }
       }
     }
@@ -213,45 +233,62 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
 
   // ---------------- store ----------------
   {
+    constexpr int kBatch = 8;
     const int units = a.nout;
     const int total = TB * units;
     const int64_t s = a.st.axis_stride;
-    for (int e = tid; e < total; e += nth) {
-      int r, i;
-      walk(e, a.st.colmap, TB, dTB, units, dOut, r, i);
-      if (r >= rows) continue;
-      const int64_t off = roff_out[r];
-      if constexpr (OP == OP_C2C) {
-        cx<T> v = res[sidx(r, i, pitch, ps)];
-        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
-        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
-      } else if constexpr (OP == OP_C2C_TW) {
-        cx<T> v = res[sidx(r, i, pitch, ps)];
-        const cx<T> w = split_twiddle<T>(reinterpret_cast<const cx<T> *>(a.aux),
-                                         reinterpret_cast<const cx<T> *>(a.aux2), a.aux_s,
-                                         uint32_t(rowaux[r]) * uint32_t(i));
-        v = mul<T>(v, w);
-        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
-        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
-      } else if constexpr (OP == OP_BLUE) {
-        const cx<T> *bk = reinterpret_cast<const cx<T> *>(a.aux);
-        // y = conj(F) * conj(bk) = conj(F * bk)
-        cx<T> v = cj<T>(mul<T>(res[sidx(r, i, pitch, ps)], bk[i]));
-        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
-        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
-      } else if constexpr (OP == OP_R2C_EVEN || OP == OP_R2C_ODD) {
-        cx<T> v = res[sidx(r, i, pitch, ps)];
-        if (OP == OP_R2C_ODD && i == 0) v.y = T(0);
-        v = mk<T>(v.x * fct, (cout ? -v.y : v.y) * fct);
-        reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v;
-      } else if constexpr (OP == OP_C2R_EVEN) {
-        // x_{2j} = Re F_j, x_{2j+1} = -Im F_j
-        const int j = i >> 1;
-        const cx<T> v = res[sidx(r, j, pitch, ps)];
-        reinterpret_cast<T *>(a.out)[off + i * s] = ((i & 1) ? -v.y : v.x) * fct;
-      } else if constexpr (OP == OP_C2R_ODD) {
-        const cx<T> v = res[sidx(r, i, pitch, ps)];
-        reinterpret_cast<T *>(a.out)[off + i * s] = v.x * fct;
+    for (int e0 = tid; e0 < total; e0 += nth * kBatch) {
+      cx<T> v[kBatch];
+      int rr[kBatch], ii[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * nth;
+        rr[u] = -1;
+        if (e < total) {
+          int r, i;
+          walk(e, a.st.colmap, TB, dTB, units, dOut, r, i);
+          if (r < rows) {
+            rr[u] = r;
+            ii[u] = i;
+            cx<T> x = res[sidx(r, i, pitch, ps)];
+            if constexpr (OP == OP_C2C_TW) {
+              x = mul<T>(x, split_twiddle<T>(reinterpret_cast<const cx<T> *>(a.aux),
+                                             reinterpret_cast<const cx<T> *>(a.aux2), a.aux_s,
+                                             uint32_t(rowaux[r]) * uint32_t(i)));
+            } else if constexpr (OP == OP_BLUE) {
+              // y = conj(F) * conj(bk) = conj(F * bk)
+              x = cj<T>(mul<T>(x, reinterpret_cast<const cx<T> *>(a.aux)[i]));
+            } else if constexpr (OP == OP_R2C_ODD) {
+              if (i == 0) x.y = T(0);
+            } else if constexpr (OP == OP_C2R_EVEN) {
+              x.y = -x.y;  // (x_2i, x_2i+1) = (Re F_i, -Im F_i)
+            }
+            if constexpr (OP == OP_C2R_EVEN || OP == OP_C2R_ODD) {
+              v[u] = mk<T>(x.x * fct, x.y * fct);
+            } else {
+              v[u] = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        if (rr[u] < 0) continue;
+        const int64_t off = roff_out[rr[u]];
+        const int i = ii[u];
+        if constexpr (OP == OP_C2R_EVEN) {
+          T *out = reinterpret_cast<T *>(a.out);
+          if (s == 1 && (reinterpret_cast<uintptr_t>(out + off) & (sizeof(cx<T>) - 1)) == 0) {
+            reinterpret_cast<cx<T> *>(out + off)[i] = v[u];
+          } else {
+            out[off + 2 * i * s] = v[u].x;
+            out[off + (2 * i + 1) * s] = v[u].y;
+          }
+        } else if constexpr (OP == OP_C2R_ODD) {
+          reinterpret_cast<T *>(a.out)[off + i * s] = v[u].x;
+        } else {
+          reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v[u];
+        }
       }
     }
   }

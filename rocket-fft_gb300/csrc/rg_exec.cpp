@@ -167,8 +167,9 @@ struct Geo {
 };
 
 // Rows per CTA, threads and shared memory for an on-chip job of core length L whose
-// shared rows need Lsm complex slots.
-Geo choose_geo(DType dt, int L, int Lsm, bool col, int64_t nrows) {
+// shared rows need Lsm complex slots. `pow2tb` keeps TB a power of two (the power-of-two
+// kernel indexes rows with masks).
+Geo choose_geo(DType dt, int L, int Lsm, bool col, int64_t nrows, bool pow2tb) {
   Geo g{};
   g.pitch = row_pitch(dt, Lsm, g.ps);
   const size_t maxsm = max_smem_optin();
@@ -177,7 +178,9 @@ Geo choose_geo(DType dt, int L, int Lsm, bool col, int64_t nrows) {
     TB = dt == DType::F32 ? 16 : 8;
   else
     TB = std::max(1, (dt == DType::F32 ? 4096 : 2048) / L);
-  if (int64_t(TB) > nrows) TB = int(std::max<int64_t>(1, nrows));
+  if (int64_t(TB) > nrows && !(pow2tb && col)) TB = int(std::max<int64_t>(1, nrows));
+  if (pow2tb)
+    while (TB & (TB - 1)) TB &= TB - 1;
   const size_t budget_soft = col ? 160 * 1024 : 112 * 1024;
   for (;;) {
     const size_t smem = smem_bytes(dt, TB, g.pitch);
@@ -189,8 +192,18 @@ Geo choose_geo(DType dt, int L, int Lsm, bool col, int64_t nrows) {
       return g;
     }
     if (TB == 1) throw Error(RG_ERR_INTERNAL, "no launch geometry for length " + std::to_string(L));
-    TB = TB > 4 ? TB - TB / 4 : TB - 1;
+    TB = pow2tb ? TB / 2 : (TB > 4 ? TB - TB / 4 : TB - 1);
   }
+}
+
+// The power-of-two kernel can be switched off (ROCKET_GPU_POW2=0) to compare against the
+// generic kernel.
+bool pow2_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("ROCKET_GPU_POW2");
+    return !(e && e[0] == '0');
+  }();
+  return on;
 }
 
 struct Job {
@@ -216,7 +229,12 @@ void run_job(const Job &j, cudaStream_t st) {
   Side ld = j.ld, sd = j.st;
   set_colmap(ld);
   set_colmap(sd);
-  const Geo g = choose_geo(j.dt, j.L, j.Lsm, ld.colmap || sd.colmap, j.nrows);
+  // power-of-two kernel: L = 2^k >= 2, ops with a direct first or last pass; a single pass
+  // whose two sides walk differently stays on the generic kernel
+  const bool pow2_op = j.op == OP_C2C || j.op == OP_C2C_TW || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN;
+  const bool pow2 = pow2_op && j.L >= 2 && (j.L & (j.L - 1)) == 0 && pow2_enabled() &&
+                    !((j.op == OP_C2C || j.op == OP_C2C_TW) && ct.core.npass == 1 && ld.colmap != sd.colmap);
+  const Geo g = choose_geo(j.dt, j.L, j.Lsm, ld.colmap || sd.colmap, j.nrows, pow2);
   KArgs a{};
   a.in = j.in;
   a.out = j.out;
@@ -243,6 +261,7 @@ void run_job(const Job &j, cudaStream_t st) {
   cfg.grid = unsigned(grid);
   cfg.threads = g.threads;
   cfg.smem = g.smem;
+  cfg.pow2 = pow2;
   launch_axis(j.dt, j.op, a, cfg, st);
 }
 
@@ -403,7 +422,7 @@ void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     j.n = int(n);
     j.L = L;
     j.Lsm = L + 1;
-    j.nin = int(n);
+    j.nin = L;  // real pairs
     j.nout = L + 1;
     j.in = in;
     j.out = out;
@@ -457,7 +476,7 @@ void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     j.L = L;
     j.Lsm = L + 1;
     j.nin = L + 1;
-    j.nout = int(n);
+    j.nout = L;  // real pairs
     j.in = in;
     j.out = out;
     j.ld = ld;

@@ -2,6 +2,11 @@
 #include "rg_launch.hpp"
 
 #include <atomic>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "rg_error.hpp"
 
@@ -19,26 +24,129 @@ static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
+// ---------------------------------------------------------------------------------------
+// event-based per-kernel profile: when enabled, every launch is bracketed by two CUDA events
+// on its own stream and its algorithmic bytes (one read of its input rows plus one write of
+// its output rows) are recorded; profile_read() synchronises and aggregates per kernel name.
+// ---------------------------------------------------------------------------------------
+
+namespace {
+struct ProfRec {
+  std::string name;
+  uint64_t bytes;
+  cudaEvent_t a, b;
+};
+std::atomic<bool> g_prof{false};
+std::mutex g_pmu;
+std::vector<ProfRec> g_pending;
+std::map<std::string, KernelStat> g_agg;
+
+const char *axis_name(int op) {
+  switch (op) {
+    case OP_C2C: return "axis_c2c";
+    case OP_C2C_TW: return "axis_c2c_twiddle";
+    case OP_R2C_EVEN: return "axis_r2c_even";
+    case OP_R2C_ODD: return "axis_r2c_odd";
+    case OP_C2R_EVEN: return "axis_c2r_even";
+    case OP_C2R_ODD: return "axis_c2r_odd";
+    case OP_BLUE: return "axis_bluestein";
+    default: return "axis_other";
+  }
+}
+const char *pw_name(int op) {
+  switch (op) {
+    case PW_BLUE_PRE: return "pw_blue_pre";
+    case PW_BLUE_MID: return "pw_blue_mid";
+    case PW_BLUE_POST: return "pw_blue_post";
+    case PW_R2C_PACK: return "pw_r2c_pack";
+    case PW_R2C_TAKE: return "pw_r2c_take";
+    case PW_C2R_BUILD: return "pw_c2r_build";
+    case PW_C2R_TAKE: return "pw_c2r_take";
+    default: return "pw_other";
+  }
+}
+
+template <class F> void timed(const std::string &name, uint64_t bytes, cudaStream_t st, F launch) {
+  if (!g_prof.load(std::memory_order_relaxed)) {
+    launch();
+    return;
+  }
+  ProfRec r{name, bytes, nullptr, nullptr};
+  RG_CUDA(cudaEventCreate(&r.a));
+  RG_CUDA(cudaEventCreate(&r.b));
+  RG_CUDA(cudaEventRecord(r.a, st));
+  launch();
+  RG_CUDA(cudaEventRecord(r.b, st));
+  std::lock_guard<std::mutex> lk(g_pmu);
+  g_pending.push_back(r);
+}
+
+uint64_t axis_bytes(DType dt, int op, const KArgs &a) {
+  const uint64_t c = cx_size(dt), r = real_size(dt);
+  // units: real pairs for the even-length real ops, single reals for the odd ones
+  const uint64_t in_unit = op == OP_R2C_EVEN ? 2 * r : op == OP_R2C_ODD ? r : c;
+  const uint64_t out_unit = op == OP_C2R_EVEN ? 2 * r : op == OP_C2R_ODD ? r : c;
+  return uint64_t(a.nrows) * (uint64_t(a.nin) * in_unit + uint64_t(a.nout) * out_unit);
+}
+}  // namespace
+
+void profile_enable(bool on) { g_prof.store(on); }
+
+std::vector<KernelStat> profile_read() {
+  std::lock_guard<std::mutex> lk(g_pmu);
+  for (ProfRec &r : g_pending) {
+    RG_CUDA(cudaEventSynchronize(r.b));
+    float ms = 0.f;
+    RG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+    KernelStat &k = g_agg[r.name];
+    std::strncpy(k.name, r.name.c_str(), sizeof(k.name) - 1);
+    k.launches += 1;
+    k.total_ms += ms;
+    k.bytes += r.bytes;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  g_pending.clear();
+  std::vector<KernelStat> out;
+  for (auto &kv : g_agg) out.push_back(kv.second);
+  return out;
+}
+
+void profile_reset() {
+  profile_read();
+  std::lock_guard<std::mutex> lk(g_pmu);
+  g_agg.clear();
+}
+
 void launch_axis(DType dt, int op, const KArgs &a, const LaunchCfg &cfg, cudaStream_t st) {
   if (cfg.grid == 0) return;
-  if (dt == DType::F32)
-    launch_axis_f32(op, a, cfg, st);
-  else
-    launch_axis_f64(op, a, cfg, st);
+  const std::string name = std::string(axis_name(op)) + (dt == DType::F32 ? "_f32" : "_f64");
+  timed(name, axis_bytes(dt, op, a), st, [&] {
+    if (dt == DType::F32)
+      launch_axis_f32(op, a, cfg, st);
+    else
+      launch_axis_f64(op, a, cfg, st);
+  });
 }
 
 void launch_pointwise(DType dt, int op, const PwArgs &a, cudaStream_t st) {
-  if (dt == DType::F32)
-    launch_pw_f32(op, a, st);
-  else
-    launch_pw_f64(op, a, st);
+  const std::string name = std::string(pw_name(op)) + (dt == DType::F32 ? "_f32" : "_f64");
+  timed(name, uint64_t(a.nrows) * uint64_t(a.nout) * 2 * cx_size(dt), st, [&] {
+    if (dt == DType::F32)
+      launch_pw_f32(op, a, st);
+    else
+      launch_pw_f64(op, a, st);
+  });
 }
 
 void launch_mirror(DType dt, const MirrorArgs &a, cudaStream_t st) {
-  if (dt == DType::F32)
-    launch_mirror_f32(a, st);
-  else
-    launch_mirror_f64(a, st);
+  timed(std::string("mirror") + (dt == DType::F32 ? "_f32" : "_f64"), uint64_t(a.total) * 2 * cx_size(dt), st,
+        [&] {
+          if (dt == DType::F32)
+            launch_mirror_f32(a, st);
+          else
+            launch_mirror_f64(a, st);
+        });
 }
 
 size_t max_smem_optin() {

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "rg_common.cuh"
 #include "rg_plan.hpp"
 
@@ -12,6 +14,7 @@ struct LaunchCfg {
   unsigned grid;
   int threads;
   size_t smem;
+  bool pow2 = false;  // use the power-of-two specialised kernel (rg_pow2_kernel.cuh)
 };
 
 // Launch axis_kernel<T, op> with the given configuration.
@@ -67,5 +70,16 @@ size_t max_smem_optin();
 
 uint64_t launch_count();
 void note_launch();
+
+// Per-kernel profile (see rocketgpu_profile_* in include/rocket_gpu.h).
+struct KernelStat {
+  char name[48] = {0};
+  uint64_t launches = 0;
+  double total_ms = 0;
+  uint64_t bytes = 0;
+};
+void profile_enable(bool on);
+std::vector<KernelStat> profile_read();
+void profile_reset();
 
 }  // namespace rg

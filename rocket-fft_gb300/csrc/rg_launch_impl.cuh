@@ -4,6 +4,7 @@
 #include <mutex>
 
 #include "rg_axis_kernel.cuh"
+#include "rg_pow2_kernel.cuh"
 #include "rg_error.hpp"
 #include "rg_launch.hpp"
 
@@ -25,11 +26,21 @@ inline void ensure_smem_attr(const void *fn, size_t smem) {
 
 template <typename T, int OP>
 void launch_axis_t(const KArgs &a, const LaunchCfg &cfg, cudaStream_t st) {
-  const void *fn = reinterpret_cast<const void *>(&axis_kernel<T, OP>);
-  ensure_smem_attr(fn, cfg.smem);
   const FastDiv dTB = make_fastdiv(uint32_t(a.TB));
   const FastDiv dIn = make_fastdiv(uint32_t(a.nin > 0 ? a.nin : 1));
   const FastDiv dOut = make_fastdiv(uint32_t(a.nout > 0 ? a.nout : 1));
+  if constexpr (OP == OP_C2C || OP == OP_C2C_TW || OP == OP_R2C_EVEN || OP == OP_C2R_EVEN) {
+    if (cfg.pow2) {
+      const void *fn = reinterpret_cast<const void *>(&pow2_kernel<T, OP>);
+      ensure_smem_attr(fn, cfg.smem);
+      pow2_kernel<T, OP><<<cfg.grid, cfg.threads, cfg.smem, st>>>(a, dTB, dIn, dOut);
+      note_launch();
+      RG_CUDA(cudaGetLastError());
+      return;
+    }
+  }
+  const void *fn = reinterpret_cast<const void *>(&axis_kernel<T, OP>);
+  ensure_smem_attr(fn, cfg.smem);
   axis_kernel<T, OP><<<cfg.grid, cfg.threads, cfg.smem, st>>>(a, dTB, dIn, dOut);
   note_launch();
   RG_CUDA(cudaGetLastError());

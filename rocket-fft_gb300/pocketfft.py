@@ -46,6 +46,9 @@ __all__ = [
     "plan_cache_bytes",
     "plan_cache_clear",
     "launch_count",
+    "profile_enable",
+    "profile_read",
+    "profile_reset",
     "version",
 ]
 
@@ -338,6 +341,24 @@ def plan_cache_clear():
 def launch_count():
     """Kernel launches issued by the library since it was loaded."""
     return int(_lib.load().rocketgpu_launch_count())
+
+
+def profile_enable(on=True):
+    """Bracket every kernel launch with CUDA events (see ``profile_read``)."""
+    _lib.load().rocketgpu_profile_enable(1 if on else 0)
+
+
+def profile_read():
+    """Per-kernel aggregates since the last reset: name, launches, device milliseconds and
+    algorithmic bytes (one read of each launch's input rows plus one write of its output)."""
+    buf = (_lib.KStat * 256)()
+    n = _lib.load().rocketgpu_profile_read(buf, 256)
+    return [{"name": buf[i].name.decode(), "launches": int(buf[i].launches), "total_ms": float(buf[i].total_ms),
+             "bytes": int(buf[i].bytes)} for i in range(n)]
+
+
+def profile_reset():
+    _lib.load().rocketgpu_profile_reset()
 
 
 def version():

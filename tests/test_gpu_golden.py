@@ -55,3 +55,19 @@ def test_golden_replay(rg, golden, cuda, where):
         if not err <= TOL[want.dtype]:
             failures.append((i, c, err))
     assert not failures, f"{len(failures)} of {len(meta)} cases fail, first: {failures[:5]}"
+
+
+def test_golden_replay_generic_kernel_only(tmp_path):
+    """The same replay with the power-of-two kernel switched off (ROCKET_GPU_POW2=0), so the
+    generic kernel stays covered for lengths the specialised one normally takes."""
+    import os
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+
+    env = dict(os.environ, ROCKET_GPU_POW2="0")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-m", "gpu",
+                        str(ROOT / "tests" / "test_gpu_golden.py") + "::test_golden_replay"],
+                       env=env, capture_output=True, text=True, cwd=str(ROOT))
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
