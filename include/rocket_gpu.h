@@ -147,6 +147,23 @@ void rocketgpu_profile_enable(int on);
 int rocketgpu_profile_read(rocketgpu_kstat_t *out, int max);
 void rocketgpu_profile_reset(void);
 
+/* Allocation-free complex FFT. No counterpart in the reference: it exists for callers that
+ * cannot allocate device memory while they run (memory-capped or pre-partitioned contexts,
+ * real-time loops that must not take the allocator's locks or fail on out-of-memory midway,
+ * hosts whose device allocator belongs to another runtime). Same transform and arguments as
+ * numba_c2c_st for DEVICE arrays of complex64/complex128, issued on `stream` (NULL = legacy
+ * default stream); every length must be 13-smooth (on chip up to 8192, or a two-pass
+ * product). It calls no cudaMalloc/cudaFree or any allocating library routine: plan tables and
+ * the long-length workspace live in one 32 MiB static device array (held by every GPU that
+ * loads the library until exit); requests that need more return RG_ERR_UNSUPPORTED without
+ * doing any work. All calls share the array: calls whose GPU work overlaps race. The first call
+ * on a device looks the array's address up (cudaGetSymbolAddress); make it before any stream
+ * capture. Returns a status; a message (if any) is copied to errbuf (at most errlen-1 bytes
+ * plus NUL; errbuf may be NULL). */
+int rocketgpu_c2c_noalloc(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                          rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads,
+                          void *stream, char *errbuf, size_t errlen);
+
 /* Library version string. */
 const char *rocketgpu_version(void);
 
