@@ -266,8 +266,28 @@ int do_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_
   });
 }
 
-int not_yet(const char *what) {
-  return guarded([&] { throw Error(RG_ERR_UNSUPPORTED, std::string(what) + " is not available in this build"); });
+// Real in, real out, same shape and dtype (dct/dst/r2r_fftpack/Hartley).
+template <class Body> int do_real(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                                  rocketgpu_arystruct_t *axes, Body body) {
+  return guarded([&] {
+    const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
+    const DType dt = real_dtype(din.itemsize);
+    RG_CHECK(dout.itemsize == din.itemsize, RG_ERR_ARG, "input and output dtypes differ");
+    check_same_shape(din, dout);
+    const auto ax = parse_axes(axes, ndim);
+    if (any_zero(din.shape) || ax.empty()) return;
+    with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) { body(dt, i, o, ax, st); });
+  });
+}
+
+int do_dcst(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+            rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho, bool cosine) {
+  if (type < 1 || type > 4)  // checked before anything else, as the reference (HDR:3896-3897, 3919-3920)
+    return guarded([&] { throw Error(RG_ERR_ARG, cosine ? "invalid DCT type" : "invalid DST type"); });
+  return do_real(ndim, ain, aout, axes, [&](DType dt, const NdArray &i, const NdArray &o, const rg::Axes &ax,
+                                            cudaStream_t st) {
+    rg::exec_dcst(dt, i, o, ax, int(type), cosine, fct, ortho, st);
+  });
 }
 
 }  // namespace
@@ -319,47 +339,53 @@ RG_EXPORT void numba_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocket
   numba_c2r_st(ndim, ain, aout, axes, forward, fct, nthreads);
 }
 
-RG_EXPORT int numba_dct_st(uint64_t, const rocketgpu_arystruct_t *, rocketgpu_arystruct_t *,
-                           rocketgpu_arystruct_t *, uint64_t, double, bool, uint64_t) {
-  return not_yet("dct");
+RG_EXPORT int numba_dct_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                           rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho, uint64_t) {
+  return do_dcst(ndim, ain, aout, axes, type, fct, ortho, true);
 }
 RG_EXPORT void numba_dct(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
                          rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
                          uint64_t nthreads) {
   numba_dct_st(ndim, ain, aout, axes, type, fct, ortho, nthreads);
 }
-RG_EXPORT int numba_dst_st(uint64_t, const rocketgpu_arystruct_t *, rocketgpu_arystruct_t *,
-                           rocketgpu_arystruct_t *, uint64_t, double, bool, uint64_t) {
-  return not_yet("dst");
+RG_EXPORT int numba_dst_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                           rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho, uint64_t) {
+  return do_dcst(ndim, ain, aout, axes, type, fct, ortho, false);
 }
 RG_EXPORT void numba_dst(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
                          rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
                          uint64_t nthreads) {
   numba_dst_st(ndim, ain, aout, axes, type, fct, ortho, nthreads);
 }
-RG_EXPORT int numba_r2r_fftpack_st(uint64_t, const rocketgpu_arystruct_t *, rocketgpu_arystruct_t *,
-                                   rocketgpu_arystruct_t *, bool, bool, double, uint64_t) {
-  return not_yet("r2r_fftpack");
+RG_EXPORT int numba_r2r_fftpack_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                                   rocketgpu_arystruct_t *axes, bool real2hermitian, bool forward, double fct,
+                                   uint64_t) {
+  return do_real(ndim, ain, aout, axes, [&](DType dt, const NdArray &i, const NdArray &o, const rg::Axes &ax,
+                                            cudaStream_t st) {
+    rg::exec_r2r_fftpack(dt, i, o, ax, real2hermitian, forward, fct, st);
+  });
 }
 RG_EXPORT void numba_r2r_fftpack(uint64_t ndim, const rocketgpu_arystruct_t *ain,
                                  rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
                                  bool real2hermitian, bool forward, double fct, uint64_t nthreads) {
   numba_r2r_fftpack_st(ndim, ain, aout, axes, real2hermitian, forward, fct, nthreads);
 }
-RG_EXPORT int numba_r2r_separable_hartley_st(uint64_t, const rocketgpu_arystruct_t *,
-                                             rocketgpu_arystruct_t *, rocketgpu_arystruct_t *, double,
+RG_EXPORT int numba_r2r_separable_hartley_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                             rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, double fct,
                                              uint64_t) {
-  return not_yet("r2r_separable_hartley");
+  return do_real(ndim, ain, aout, axes, [&](DType dt, const NdArray &i, const NdArray &o, const rg::Axes &ax,
+                                            cudaStream_t st) { rg::exec_hartley(dt, i, o, ax, false, fct, st); });
 }
 RG_EXPORT void numba_r2r_separable_hartley(uint64_t ndim, const rocketgpu_arystruct_t *ain,
                                            rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
                                            double fct, uint64_t nthreads) {
   numba_r2r_separable_hartley_st(ndim, ain, aout, axes, fct, nthreads);
 }
-RG_EXPORT int numba_r2r_genuine_hartley_st(uint64_t, const rocketgpu_arystruct_t *,
-                                           rocketgpu_arystruct_t *, rocketgpu_arystruct_t *, double,
+RG_EXPORT int numba_r2r_genuine_hartley_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                           rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, double fct,
                                            uint64_t) {
-  return not_yet("r2r_genuine_hartley");
+  return do_real(ndim, ain, aout, axes, [&](DType dt, const NdArray &i, const NdArray &o, const rg::Axes &ax,
+                                            cudaStream_t st) { rg::exec_hartley(dt, i, o, ax, true, fct, st); });
 }
 RG_EXPORT void numba_r2r_genuine_hartley(uint64_t ndim, const rocketgpu_arystruct_t *ain,
                                          rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,

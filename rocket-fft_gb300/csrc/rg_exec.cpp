@@ -18,6 +18,7 @@
 #include <mutex>
 
 #include "rg_error.hpp"
+#include "rg_exec_detail.hpp"
 #include "rg_launch.hpp"
 
 namespace rg {
@@ -59,12 +60,7 @@ void pool_trim() { cudaMemPoolTrimTo(device_pool(), 0); }
 // batch geometry
 // ---------------------------------------------------------------------------------------
 
-namespace {
-
-struct Batch {
-  std::vector<int64_t> shape, s_in, s_out;  // fastest first after sorting and merging
-  int64_t nrows = 1;
-};
+namespace detail {
 
 Batch make_batch(const std::vector<int64_t> &shape, const std::vector<int64_t> &s_in,
                  const std::vector<int64_t> &s_out, int axis) {
@@ -522,7 +518,9 @@ bool any_zero(const std::vector<int64_t> &shape) {
   return false;
 }
 
-}  // namespace
+}  // namespace detail
+
+using namespace detail;
 
 // ---------------------------------------------------------------------------------------
 // public driver

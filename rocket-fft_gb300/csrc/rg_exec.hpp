@@ -29,6 +29,14 @@ void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
 void exec_c2c_sym(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
                   double fct, cudaStream_t st);
 
+// Real-to-real transforms (rg_r2r.cu): DCT (cosine) / DST types 1-4, FFTPACK r2r, Hartley.
+void exec_dcst(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, int type, bool cosine,
+               double fct, bool ortho, cudaStream_t st);
+void exec_r2r_fftpack(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool real2hermitian,
+                      bool forward, double fct, cudaStream_t st);
+void exec_hartley(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool genuine, double fct,
+                  cudaStream_t st);
+
 // Device workspace from a per-device stream-ordered pool.
 class DevBuf {
  public:

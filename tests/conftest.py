@@ -60,6 +60,21 @@ def cuda():
     return torch
 
 
+def run_golden_case(api, c, x, out):
+    """Run golden case `c` (see tests/golden/make_golden.py) through `api`, which is the
+    package or an oracle: both take the reference's low-level signatures."""
+    k = c["kind"]
+    axes = np.array(c["axes"], dtype=np.int64)
+    if k in ("c2c", "r2c", "c2r", "c2c_sym"):
+        getattr(api, k)(x, out, axes, bool(c["forward"]), float(c["fct"]), 1)
+    elif k in ("dct", "dst"):
+        getattr(api, k)(x, out, axes, int(c["type"]), float(c["fct"]), bool(c["ortho"]), 1)
+    elif k == "r2r_fftpack":
+        api.r2r_fftpack(x, out, axes, bool(c["real2hermitian"]), bool(c["forward"]), float(c["fct"]), 1)
+    else:
+        getattr(api, k)(x, out, axes, float(c["fct"]), 1)
+
+
 # tolerances of relative L2 error: single and double precision
 TOL = {np.dtype(np.float32): 1e-6, np.dtype(np.complex64): 1e-6,
        np.dtype(np.float64): 1e-13, np.dtype(np.complex128): 1e-13}

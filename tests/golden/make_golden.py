@@ -49,6 +49,24 @@ def cases():
                     out.append(dict(kind="r2c", prec=prec, shape=list(shp), axes=axes, forward=fwd, fct=1.0))
                     out.append(dict(kind="c2r", prec=prec, shape=list(shp), axes=axes, forward=fwd, fct=2.0))
                     out.append(dict(kind="c2c_sym", prec=prec, shape=list(shp), axes=axes, forward=fwd, fct=1.0))
+    # real-to-real transforms (DCT/DST I-IV x ortho, r2r_fftpack flags, Hartley forms)
+    r_lens = [1, 2, 3, 4, 5, 7, 8, 9, 16, 17, 31, 64, 100, 127, 128, 243, 512, 1000]
+    r_shapes = [((16, 17), [0, 1]), ((16, 17), [1]), ((8, 5, 7), [2, 0]), ((9, 8), [1, 0])]
+    for prec in ("f64", "f32"):
+        geoms = [([n], [0]) for n in r_lens] + [(list(sh), ax) for sh, ax in r_shapes]
+        for shape, axes in geoms:
+            for kind in ("dct", "dst"):
+                for t in (1, 2, 3, 4):
+                    if kind == "dct" and t == 1 and any(shape[a] == 1 for a in axes):
+                        continue
+                    for ortho in (False, True):
+                        out.append(dict(kind=kind, prec=prec, shape=shape, axes=axes, type=t, ortho=ortho, fct=0.5))
+            for r2h in (True, False):
+                for fw in (True, False):
+                    out.append(dict(kind="r2r_fftpack", prec=prec, shape=shape, axes=axes, real2hermitian=r2h,
+                                    forward=fw, fct=1.0))
+            for kind in ("r2r_separable_hartley", "r2r_genuine_hartley"):
+                out.append(dict(kind=kind, prec=prec, shape=shape, axes=axes, fct=1.0))
     return out
 
 
@@ -72,6 +90,18 @@ def run_case(c, rng, R):
         x = (rng.standard_normal(ishape) + 1j * rng.standard_normal(ishape)).astype(CDT[prec])
         y = np.empty(shape, RDT[prec])
         R.c2r(x, y, axes, c["forward"], c["fct"])
+    elif kind in ("dct", "dst"):
+        x = rng.standard_normal(shape).astype(RDT[prec])
+        y = np.empty_like(x)
+        getattr(R, kind)(x, y, axes, c["type"], c["fct"], c["ortho"])
+    elif kind == "r2r_fftpack":
+        x = rng.standard_normal(shape).astype(RDT[prec])
+        y = np.empty_like(x)
+        R.r2r_fftpack(x, y, axes, c["real2hermitian"], c["forward"], c["fct"])
+    elif kind in ("r2r_separable_hartley", "r2r_genuine_hartley"):
+        x = rng.standard_normal(shape).astype(RDT[prec])
+        y = np.empty_like(x)
+        getattr(R, kind)(x, y, axes, c["fct"])
     else:
         raise ValueError(kind)
     return x, y

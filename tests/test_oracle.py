@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import run_golden_case
 
 TOL = {"f32": 1e-6, "f64": 1e-13}
 RDT = {"f32": np.float32, "f64": np.float64}
@@ -32,7 +33,7 @@ def test_port_matches_golden(P, golden):
     for i, c in enumerate(meta):
         x, want = data[f"in_{i}"], data[f"out_{i}"]
         got = np.empty_like(want)
-        getattr(P, c["kind"])(x.copy(), got, c["axes"], c["forward"], c["fct"])
+        run_golden_case(P, c, x.copy(), got)
         e = oracle.rel_l2(got, want)
         if not e <= TOL[c["prec"]]:
             bad.append((i, c, e))
