@@ -120,6 +120,164 @@ def dist_init():
     return world, rank, local
 
 
+def timed_steps(torch, step, steps, warmup, local, world):
+    """Run `warmup` untimed steps, then time exactly `steps` steps on the current stream with
+    CUDA events between barriers, sampling clocks meanwhile. Returns (ms, clocks, launches)."""
+    rg = load_package()
+    for i in range(warmup):
+        step(i)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = rg.launch_count()
+    stream = torch.cuda.current_stream()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        start.record(stream)
+        for i in range(steps):
+            step(i)
+        stop.record(stream)
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, clk.summary(), rg.launch_count() - launches0
+
+
+def kernel_profile(step, steps):
+    """Per-kernel device time and algorithmic bytes over `steps` steps (events around every
+    launch of the library); returns (stats, roofline dict of the dominant kernel)."""
+    rg = load_package()
+    rg.profile_reset()
+    rg.profile_enable(True)
+    for i in range(steps):
+        step(i)
+    stats = rg.profile_read()
+    rg.profile_enable(False)
+    total_ms = sum(s["total_ms"] for s in stats) or 1.0
+    dom = max(stats, key=lambda s: s["total_ms"])
+    achieved = dom["bytes"] / dom["launches"] / (dom["total_ms"] / dom["launches"] / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    roof = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": NCU_TRAFFIC.get(dom["name"]),
+            "launch_ms": dom["total_ms"] / dom["launches"], "bytes_per_launch": dom["bytes"] // dom["launches"],
+            "share": dom["total_ms"] / total_ms}
+    kernels = [{"name": s["name"], "launches": s["launches"], "ms": s["total_ms"], "share": s["total_ms"] / total_ms,
+                "gbs": s["bytes"] / (s["total_ms"] / 1e3) / 1e9 if s["total_ms"] else None} for s in stats]
+    return kernels, roof
+
+
+def base_line(metric, value, unit, world, args, ms, dtype, config):
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)", "config": config}
+
+
+def run_c1(args):
+    """Config 1: c2c complex128, batch 256 x length 4096, axes [1], forward, fct 1."""
+    import torch
+
+    import oracle
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    rg = load_package()
+    shape, axes = (256, 4096), np.array([1], dtype=np.int64)
+    rot = 16  # 16 x 16.8 MB > L2
+    gen = torch.Generator(device="cuda").manual_seed(7 + rank)
+    xs = [torch.complex(torch.randn(shape, device="cuda", dtype=torch.float64, generator=gen),
+                        torch.randn(shape, device="cuda", dtype=torch.float64, generator=gen)) for _ in range(rot)]
+    ys = [torch.empty_like(x) for x in xs]
+
+    def step(i):
+        rg.c2c(xs[i % rot], ys[i % rot], axes, True, 1.0, 1)
+
+    ms, clocks, launches = timed_steps(torch, step, args.steps, args.warmup, local, world)
+    value = world * 256 * args.steps / (ms / 1e3)
+    kernels, roof = kernel_profile(step, args.steps)
+    x0 = xs[0].cpu().numpy()
+    step(0)
+    torch.cuda.synchronize()
+    want = np.empty_like(x0)
+    cores = os.cpu_count() or 1
+    P = oracle.port()
+    P.c2c(x0, want, [1], True, 1.0, cores)
+    acc = {"rel_l2_vs_port_fp64": oracle.rel_l2(ys[0].cpu().numpy(), want)}
+    t0 = time.perf_counter()
+    for _ in range(5):
+        P.c2c(x0, want, [1], True, 1.0, cores)
+    cpu_rate = 5 * 256 / (time.perf_counter() - t0)
+    hx = torch.empty(shape, dtype=torch.complex128, pin_memory=True)
+    hx.copy_(xs[0].cpu())
+    hy = torch.empty_like(hx)
+    nx, ny = hx.numpy(), hy.numpy()
+    rg.set_stream(None)
+    rg.c2c(nx, ny, axes, True, 1.0, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rg.c2c(nx, ny, axes, True, 1.0, 1)
+    e2e_rate = 256 * args.steps / (time.perf_counter() - t0)
+    flops = 5 * 4096 * 12 * 256
+    line = base_line(METRIC, value, "transforms/s", world, args, ms, "f64",
+                     {"workload": "c2c complex128 256 x 4096, axes [1], forward, fct 1", "global_batch": 256 * world,
+                      "l2": f"inputs rotate over {rot} arrays ({rot * 16.8:.0f} MB) > L2",
+                      "fp64_tflops": flops * args.steps / (ms / 1e3) / 1e12})
+    line.update({"roofline": roof, "kernels": kernels, "accuracy": acc,
+                 "cpu_baseline": {"value": cpu_rate, "unit": "transforms/s", "cores": cores, "kind": "port",
+                                  "sample": f"5 calls of 256 x 4096, nthreads={cores}"},
+                 "e2e": {"value": e2e_rate, "unit": "transforms/s", "h2d_bytes_per_step": int(nx.nbytes),
+                         "d2h_bytes_per_step": int(ny.nbytes)},
+                 "gpu_launches": launches, "clocks": clocks})
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_c4(args):
+    """Config 4: differentiable rfftn float32 64 x 1024 x 1024 over axes (1, 2); loss =
+    sum |W * rfftn(x)|^2; gradient by the adjoint kernel (c2r with halved interior bins)."""
+    import importlib
+
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    load_package()
+    ops = importlib.import_module("rocket_fft_gb300.torch_ops")
+    shape, axes = (64, 1024, 1024), (1, 2)
+    gen = torch.Generator(device="cuda").manual_seed(11 + rank)
+    xs = [torch.randn(shape, device="cuda", generator=gen).requires_grad_(True) for _ in range(2)]
+    W = torch.complex(torch.randn((64, 1024, 513), device="cuda", generator=gen),
+                      torch.randn((64, 1024, 513), device="cuda", generator=gen))
+
+    def step(i):
+        x = xs[i % 2]
+        x.grad = None
+        loss = (W * ops.rfftn(x, axes)).abs().square().sum()
+        loss.backward()
+
+    ms, clocks, launches = timed_steps(torch, step, args.steps, args.warmup, local, world)
+    value = world * 128 * args.steps / (ms / 1e3)  # 64 forward + 64 adjoint transforms per step
+    kernels, roof = kernel_profile(step, args.steps)
+    # gradient check against torch.fft autograd on one 1024^2 slice (CPU, float64)
+    x0 = xs[0].detach()[:1].double().cpu().requires_grad_(True)
+    (W[:1].cpu().to(torch.complex128) * torch.fft.rfftn(x0, dim=axes)).abs().square().sum().backward()
+    xg = xs[0].detach()[:1].clone().requires_grad_(True)
+    (W[:1] * ops.rfftn(xg, axes)).abs().square().sum().backward()
+    err = float((xg.grad.double().cpu() - x0.grad).norm() / x0.grad.norm())
+    line = base_line(METRIC, value, "transforms/s", world, args, ms, "f32",
+                     {"workload": "rfftn float32 64 x 1024 x 1024 axes (1,2), loss sum|W*X|^2, forward + adjoint",
+                      "global_batch": 64 * world, "l2": "2 rotating 256 MiB inputs > L2"})
+    line.update({"roofline": roof, "kernels": kernels, "accuracy": {"grad_rel_l2_vs_torch_fp64": err},
+                 "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clocks})
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def cpu_round_trip_rate(P, nthreads, reps, rng):
     """Transforms/s of the oracle port on the host: `reps` round trips of the 256^3 volume."""
     x = rng.uniform(-1, 1, SHAPE).astype(np.float32)
@@ -308,9 +466,16 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c4"],
+                    help="c2 (default): the 256^3 round trip the metric is quoted on; c1, c4: other "
+                         "BASELINE configurations")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "c1":
+        run_c1(args)
+    elif args.config == "c4":
+        run_c4(args)
     else:
         run_ours(args)
 

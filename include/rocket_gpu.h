@@ -110,6 +110,23 @@ int numba_r2r_genuine_hartley_st(uint64_t ndim, const rocketgpu_arystruct_t *ain
                                  rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
                                  double fct, uint64_t nthreads);
 
+/* ---- adjoints for automatic differentiation (no reference counterpart) ----
+ * Same arguments as the transform whose adjoint they compute; ain is the cotangent of that
+ * transform's output, aout receives the cotangent of its input.
+ *   rocketgpu_r2c_adjoint_st: adjoint of numba_r2c -- a c2r in the opposite direction with the
+ *     interior half-spectrum bins (0 < k < n/2) of the last axis halved; ain half spectrum,
+ *     aout real.
+ *   rocketgpu_c2r_adjoint_st: adjoint of numba_c2r -- an r2c in the opposite direction with
+ *     those bins doubled; ain real, aout half spectrum.
+ *   rocketgpu_dct_adjoint_st: transpose of numba_dct (types 1-4). */
+int rocketgpu_r2c_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                             rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+int rocketgpu_c2r_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                             rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads);
+int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                             rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
+                             uint64_t nthreads);
+
 /* ---- runtime control (no reference counterpart) ---- */
 
 /* Status and message of the calling thread's most recent call (RG_OK / "" after success).

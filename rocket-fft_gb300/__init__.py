@@ -12,7 +12,9 @@ from .pocketfft import (  # noqa: F401
     c2c,
     c2c_sym,
     c2r,
+    c2r_adjoint,
     dct,
+    dct_adjoint,
     dst,
     good_size,
     launch_count,
@@ -23,6 +25,7 @@ from .pocketfft import (  # noqa: F401
     profile_read,
     profile_reset,
     r2c,
+    r2c_adjoint,
     r2r_fftpack,
     r2r_genuine_hartley,
     r2r_separable_hartley,

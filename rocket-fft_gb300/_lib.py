@@ -58,10 +58,11 @@ def _declare(lib):
     u64, i32, dbl, b = ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_bool
     cm = [u64, P, P, P, b, dbl, u64]
     rl = [u64, P, P, P, u64, dbl, b, u64]
-    for name in ("numba_c2c_st", "numba_r2c_st", "numba_c2r_st", "numba_c2c_sym_st"):
+    for name in ("numba_c2c_st", "numba_r2c_st", "numba_c2r_st", "numba_c2c_sym_st", "rocketgpu_r2c_adjoint_st",
+                 "rocketgpu_c2r_adjoint_st"):
         getattr(lib, name).argtypes = cm
         getattr(lib, name).restype = i32
-    for name in ("numba_dct_st", "numba_dst_st"):
+    for name in ("numba_dct_st", "numba_dst_st", "rocketgpu_dct_adjoint_st"):
         getattr(lib, name).argtypes = rl
         getattr(lib, name).restype = i32
     lib.numba_r2r_fftpack_st.argtypes = [u64, P, P, P, b, b, dbl, u64]

@@ -229,7 +229,7 @@ int do_c2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_
 }
 
 int do_r2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
-           rocketgpu_arystruct_t *axes, bool forward, double fct, bool sym) {
+           rocketgpu_arystruct_t *axes, bool forward, double fct, bool sym, double bscale = 1.0) {
   return guarded([&] {
     const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
     const DType dt = real_dtype(din.itemsize);
@@ -245,13 +245,13 @@ int do_r2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_
       if (sym)
         rg::exec_c2c_sym(dt, i, o, ax, forward, fct, st);
       else
-        rg::exec_r2c(dt, i, o, ax, forward, fct, st);
+        rg::exec_r2c(dt, i, o, ax, forward, fct, st, bscale);
     });
   });
 }
 
 int do_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
-           rocketgpu_arystruct_t *axes, bool forward, double fct) {
+           rocketgpu_arystruct_t *axes, bool forward, double fct, double bscale = 1.0) {
   return guarded([&] {
     const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
     const DType dt = complex_dtype(din.itemsize);
@@ -261,7 +261,7 @@ int do_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_
     check_half_shape(dout, din, ax);
     if (any_zero(dout.shape)) return;
     with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
-      rg::exec_c2r(dt, i, o, ax, forward, fct, st);
+      rg::exec_c2r(dt, i, o, ax, forward, fct, st, bscale);
     });
   });
 }
@@ -281,12 +281,13 @@ template <class Body> int do_real(uint64_t ndim, const rocketgpu_arystruct_t *ai
 }
 
 int do_dcst(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
-            rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho, bool cosine) {
+            rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho, bool cosine,
+            bool adjoint = false) {
   if (type < 1 || type > 4)  // checked before anything else, as the reference (HDR:3896-3897, 3919-3920)
     return guarded([&] { throw Error(RG_ERR_ARG, cosine ? "invalid DCT type" : "invalid DST type"); });
   return do_real(ndim, ain, aout, axes, [&](DType dt, const NdArray &i, const NdArray &o, const rg::Axes &ax,
                                             cudaStream_t st) {
-    rg::exec_dcst(dt, i, o, ax, int(type), cosine, fct, ortho, st);
+    rg::exec_dcst(dt, i, o, ax, int(type), cosine, fct, ortho, st, adjoint);
   });
 }
 
@@ -391,6 +392,33 @@ RG_EXPORT void numba_r2r_genuine_hartley(uint64_t ndim, const rocketgpu_arystruc
                                          rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes,
                                          double fct, uint64_t nthreads) {
   numba_r2r_genuine_hartley_st(ndim, ain, aout, axes, fct, nthreads);
+}
+
+// ---------------------------------------------------------------------------------------
+// adjoints (no reference counterpart; used by the torch.autograd wrappers)
+// ---------------------------------------------------------------------------------------
+
+// Adjoint of numba_r2c(., forward, fct): c2r in the opposite direction with the interior bins
+// of the last axis halved. ain is the half spectrum (cotangent), aout the real gradient.
+RG_EXPORT int rocketgpu_r2c_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                       rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, bool forward,
+                                       double fct, uint64_t) {
+  return do_c2r(ndim, ain, aout, axes, !forward, fct, 0.5);
+}
+
+// Adjoint of numba_c2r(., forward, fct): r2c in the opposite direction with the interior bins
+// of the last axis doubled. ain is the real cotangent, aout the half-spectrum gradient.
+RG_EXPORT int rocketgpu_c2r_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                       rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, bool forward,
+                                       double fct, uint64_t) {
+  return do_r2c(ndim, ain, aout, axes, !forward, fct, false, 2.0);
+}
+
+// Adjoint (transpose) of numba_dct(., type, fct, ortho).
+RG_EXPORT int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain,
+                                       rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, uint64_t type,
+                                       double fct, bool ortho, uint64_t) {
+  return do_dcst(ndim, ain, aout, axes, type, fct, ortho, true, true);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
   const int tid = threadIdx.x, nth = blockDim.x;
   const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
   const T fct = T(a.fct);
+  const T bsc = T(a.bscale);
 
   for (int r = tid; r < rows; r += nth) {
     roff_in[r] = side_offset(a.ld, row0 + r);
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
           // units = L+1 Hermitian bins; imaginary parts of bins 0 and L are ignored
           if (cin) x.y = -x.y;
           if (i == 0 || i == L) x.y = T(0);
+          else x = scl<T>(x, bsc);
           sm[sidx(r, i, pitch, ps)] = x;
         } else if constexpr (OP == OP_C2R_ODD) {
           // units = (n+1)/2 bins; build conj of the full Hermitian spectrum:
@@ -144,6 +146,7 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
           if (i == 0) {
             sm[sidx(r, 0, pitch, ps)] = mk<T>(x.x, T(0));
           } else {
+            x = scl<T>(x, bsc);
             sm[sidx(r, i, pitch, ps)] = cj<T>(x);
             sm[sidx(r, L - i, pitch, ps)] = x;
           }
@@ -260,6 +263,9 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
               x = cj<T>(mul<T>(x, reinterpret_cast<const cx<T> *>(a.aux)[i]));
             } else if constexpr (OP == OP_R2C_ODD) {
               if (i == 0) x.y = T(0);
+              else x = scl<T>(x, bsc);
+            } else if constexpr (OP == OP_R2C_EVEN) {
+              if (i != 0 && i != L) x = scl<T>(x, bsc);
             } else if constexpr (OP == OP_C2R_EVEN) {
               x.y = -x.y;  // (x_2i, x_2i+1) = (Re F_i, -Im F_i)
             }

@@ -92,6 +92,8 @@ struct KArgs {
   int conj_out;    // conjugated data) / while storing
   int flags;       // op-specific (cosine/ortho/type bits, ...)
   double fct;      // scale applied to every output
+  double bscale;   // r2c/c2r: extra scale of the interior half-spectrum bins 0 < k < n/2 (1 for
+                   // the transforms; 2 / 0.5 for the adjoints of c2r / r2c)
   const void *aux;   // op-specific table (split twiddles, chirp, ...)
   const void *aux2;  // op-specific second table (Bluestein spectrum, ...)
   int aux_n;         // op-specific integer (four-step: number of columns)

@@ -217,6 +217,7 @@ struct Job {
   double fct;
   const void *aux = nullptr, *aux2 = nullptr;
   int aux_n = 1, aux_s = 0;
+  double bscale = 1.0;  // interior half-spectrum bin scale (r2c/c2r adjoints)
 };
 
 void run_job(const Job &j, cudaStream_t st) {
@@ -250,20 +251,22 @@ void run_job(const Job &j, cudaStream_t st) {
   a.aux2 = j.aux2;
   a.aux_n = j.aux_n;
   a.aux_s = j.aux_s;
+  a.bscale = j.bscale;
   a.core = ct.core;
+  const size_t smem = g.smem;
   LaunchCfg cfg;
   const int64_t grid = (j.nrows + g.TB - 1) / g.TB;
   RG_CHECK(grid < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "too many transforms in one call");
   cfg.grid = unsigned(grid);
   cfg.threads = g.threads;
-  cfg.smem = g.smem;
+  cfg.smem = smem;
   cfg.pow2 = pow2;
   launch_axis(j.dt, j.op, a, cfg, st);
 }
 
 void pointwise(DType dt, int op, const void *in, const Side &ld, void *out, const Side &sd,
                int64_t nrows, int nout, int n, bool cin, bool cout, double fct, const void *aux,
-               const void *aux2, cudaStream_t st) {
+               const void *aux2, cudaStream_t st, double bscale = 1.0) {
   PwArgs p{};
   p.in = in;
   p.out = out;
@@ -275,6 +278,7 @@ void pointwise(DType dt, int op, const void *in, const Side &ld, void *out, cons
   p.conj_in = cin;
   p.conj_out = cout;
   p.fct = fct;
+  p.bscale = bscale;
   p.aux = aux;
   p.aux2 = aux2;
   launch_pointwise(dt, op, p, st);
@@ -408,7 +412,7 @@ void c2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
 
 // real -> half-complex along rows; conj_out conjugates (reference: forward=false)
 void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
-              int64_t nrows, bool cout, double fct, cudaStream_t st) {
+              int64_t nrows, bool cout, double fct, cudaStream_t st, double bscale) {
   RG_CHECK(n < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
   if (n % 2 == 0 && fits_core(n / 2, dt)) {
     const int L = int(n / 2);
@@ -428,6 +432,7 @@ void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     j.cin = false;
     j.cout = cout;
     j.fct = fct;
+    j.bscale = bscale;
     j.aux = get_roots(uint64_t(n), uint64_t(L / 2 + 1), dt);
     run_job(j, st);
     return;
@@ -436,6 +441,7 @@ void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     Job j{};
     j.dt = dt;
     j.op = OP_R2C_ODD;
+    j.bscale = bscale;
     j.n = j.L = j.Lsm = j.nin = int(n);
     j.nout = int(n / 2 + 1);
     j.in = in;
@@ -456,12 +462,12 @@ void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
             nullptr, st);
   c2c_rows(dt, n, ws.get(), w, ws.get(), w, nrows, false, false, 1.0, st);
   pointwise(dt, PW_R2C_TAKE, ws.get(), w, out, sd, nrows, int(n / 2 + 1), int(n), false, cout, fct,
-            nullptr, nullptr, st);
+            nullptr, nullptr, st, bscale);
 }
 
 // half-complex -> real along rows; conj_in conjugates the input (reference: forward=true)
 void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
-              int64_t nrows, bool cin, double fct, cudaStream_t st) {
+              int64_t nrows, bool cin, double fct, cudaStream_t st, double bscale) {
   RG_CHECK(n < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
   if (n % 2 == 0 && fits_core(n / 2, dt)) {
     const int L = int(n / 2);
@@ -481,6 +487,7 @@ void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     j.cin = cin;
     j.cout = false;
     j.fct = fct;
+    j.bscale = bscale;
     j.aux = get_roots(uint64_t(n), uint64_t(L / 2 + 1), dt);
     run_job(j, st);
     return;
@@ -489,6 +496,7 @@ void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     Job j{};
     j.dt = dt;
     j.op = OP_C2R_ODD;
+    j.bscale = bscale;
     j.n = j.L = j.Lsm = int(n);
     j.nin = int(n / 2 + 1);
     j.nout = int(n);
@@ -506,7 +514,7 @@ void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
   DevBuf ws(size_t(nrows) * size_t(n) * cx_size(dt), st);
   const Side w = contiguous_rows(nrows, n);
   pointwise(dt, PW_C2R_BUILD, in, ld, ws.get(), w, nrows, int(n), int(n), cin, false, 1.0, nullptr,
-            nullptr, st);
+            nullptr, st, bscale);
   c2c_rows(dt, n, ws.get(), w, ws.get(), w, nrows, false, false, 1.0, st);
   pointwise(dt, PW_C2R_TAKE, ws.get(), w, out, sd, nrows, int(n), int(n), false, false, fct, nullptr,
             nullptr, st);
@@ -541,13 +549,13 @@ void exec_c2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
 }
 
 void exec_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
-              double fct, cudaStream_t st) {
+              double fct, cudaStream_t st, double bscale) {
   if (any_zero(in.shape) || axes.empty()) return;
   const int last = int(axes.back());
   const Batch b = make_batch(in.shape, in.stride, out.stride, last);
   const Side ld = make_side(in.stride[last], b.shape, b.s_in);
   const Side sd = make_side(out.stride[last], b.shape, b.s_out);
-  r2c_rows(dt, in.shape[last], in.data, ld, out.data, sd, b.nrows, !forward, fct, st);
+  r2c_rows(dt, in.shape[last], in.data, ld, out.data, sd, b.nrows, !forward, fct, st, bscale);
   if (axes.size() > 1) {
     NdArray o = out;
     o.shape = in.shape;
@@ -557,7 +565,7 @@ void exec_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
 }
 
 void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
-              double fct, cudaStream_t st) {
+              double fct, cudaStream_t st, double bscale) {
   if (any_zero(out.shape) || axes.empty()) return;
   const int last = int(axes.back());
   std::vector<int64_t> shape_in = out.shape;
@@ -566,7 +574,7 @@ void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
     const Batch b = make_batch(out.shape, in.stride, out.stride, last);
     const Side ld = make_side(in.stride[last], b.shape, b.s_in);
     const Side sd = make_side(out.stride[last], b.shape, b.s_out);
-    c2r_rows(dt, out.shape[last], in.data, ld, out.data, sd, b.nrows, forward, fct, st);
+    c2r_rows(dt, out.shape[last], in.data, ld, out.data, sd, b.nrows, forward, fct, st, bscale);
     return;
   }
   // C-contiguous complex temporary with the input's shape
@@ -584,7 +592,7 @@ void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
   const Batch b = make_batch(out.shape, t.stride, out.stride, last);
   const Side ld = make_side(t.stride[last], b.shape, b.s_in);
   const Side sd = make_side(out.stride[last], b.shape, b.s_out);
-  c2r_rows(dt, out.shape[last], t.data, ld, out.data, sd, b.nrows, forward, fct, st);
+  c2r_rows(dt, out.shape[last], t.data, ld, out.data, sd, b.nrows, forward, fct, st, bscale);
 }
 
 void exec_c2c_sym(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,

@@ -22,16 +22,21 @@ using Axes = std::vector<uint64_t>;
 
 void exec_c2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
               double fct, cudaStream_t st);
+// bscale: extra scale of the interior half-spectrum bins along the last axis (0 < k < n/2):
+// 1 for the transforms themselves, 2 for r2c as the adjoint of c2r, 0.5 for c2r as the
+// adjoint of r2c (the Hermitian bin weighting).
 void exec_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
-              double fct, cudaStream_t st);
+              double fct, cudaStream_t st, double bscale = 1.0);
 void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
-              double fct, cudaStream_t st);
+              double fct, cudaStream_t st, double bscale = 1.0);
 void exec_c2c_sym(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
                   double fct, cudaStream_t st);
 
 // Real-to-real transforms (rg_r2r.cu): DCT (cosine) / DST types 1-4, FFTPACK r2r, Hartley.
+// adjoint: the transpose of the transform (DCT/DST-II <-> III with the element-0 weight of the
+// transpose; types 1 and 4 are symmetric).
 void exec_dcst(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, int type, bool cosine,
-               double fct, bool ortho, cudaStream_t st);
+               double fct, bool ortho, cudaStream_t st, bool adjoint = false);
 void exec_r2r_fftpack(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool real2hermitian,
                       bool forward, double fct, cudaStream_t st);
 void exec_hartley(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool genuine, double fct,

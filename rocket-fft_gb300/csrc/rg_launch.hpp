@@ -43,6 +43,7 @@ struct PwArgs {
   int n;           // logical transform length
   int conj_in, conj_out;
   double fct;
+  double bscale;  // interior half-spectrum bin scale (PW_R2C_TAKE, PW_C2R_BUILD)
   const void *aux, *aux2;
 };
 

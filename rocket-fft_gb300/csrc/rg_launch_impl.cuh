@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(256) pointwise_kernel(const __grid_constant__ 
       } else if constexpr (OP == PW_R2C_TAKE) {
         cx<T> v = reinterpret_cast<const cx<T> *>(a.in)[oi + i * si];
         if (i == 0 || 2 * i == n) v.y = T(0);
+        else v = scl<T>(v, T(a.bscale));
         reinterpret_cast<cx<T> *>(a.out)[oo + i * so] = mk<T>(v.x * fct, (a.conj_out ? -v.y : v.y) * fct);
       } else if constexpr (OP == PW_C2R_BUILD) {
         const cx<T> *in = reinterpret_cast<const cx<T> *>(a.in);
@@ -104,11 +105,12 @@ __global__ void __launch_bounds__(256) pointwise_kernel(const __grid_constant__ 
           cx<T> x = in[oi + i * si];
           if (a.conj_in) x.y = -x.y;
           if (i == 0 || 2 * i == n) x.y = T(0);
+          else x = scl<T>(x, T(a.bscale));
           w = cj<T>(x);
         } else {
           cx<T> x = in[oi + (n - i) * si];
           if (a.conj_in) x.y = -x.y;
-          w = x;
+          w = scl<T>(x, T(a.bscale));
         }
         reinterpret_cast<cx<T> *>(a.out)[oo + i * so] = w;
       } else if constexpr (OP == PW_C2R_TAKE) {

@@ -160,6 +160,7 @@ __global__ void __launch_bounds__(512) pow2_kernel(const __grid_constant__ KArgs
       cx<T> x = __ldg(reinterpret_cast<const cx<T> *>(a.in) + roff_in[r] + i * s);
       if (a.conj_in) x.y = -x.y;
       if (i == 0 || i == L) x.y = T(0);
+      else x = scl<T>(x, T(a.bscale));
       sm[sidx(r, i, c.pitch, c.ps)] = x;
     }
     __syncthreads();
@@ -242,7 +243,8 @@ __global__ void __launch_bounds__(512) pow2_kernel(const __grid_constant__ KArgs
         int r, i;
         walk(e, a.st.colmap, c.TB, dTB, units, dOut, r, i);
         if (r >= c.rows) continue;
-        const cx<T> x = cur[sidx(r, i, c.pitch, c.ps)];
+        cx<T> x = cur[sidx(r, i, c.pitch, c.ps)];
+        if (i != 0 && i != L) x = scl<T>(x, T(a.bscale));
         reinterpret_cast<cx<T> *>(a.out)[roff_out[r] + i * s] = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
       }
     }

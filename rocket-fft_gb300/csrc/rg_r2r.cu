@@ -41,9 +41,12 @@ struct R2RArgs {
   int64_t nrows;
   int n;              // transform length
   int M;              // complex workspace length per row
-  int cosine, ortho;  // DCT vs DST; ortho flag
+  int cosine;         // DCT vs DST
   int neg;            // fftpack: negate entries 2,4,... (pre for r2hc, post for hc2r)
   double fct;
+  double e0, e1;      // element weights: DCT-I input ends (e0) / output ends (e1); DCT-II output
+                      // element 0 (e0); DCT-III input element 0 (e0). From `ortho`, or the
+                      // transposes' weights for the adjoints.
   const void *wa;     // W_{4n}^k, k < n   (DCT-II/III/IV)
   const void *wb;     // W_{8n}^k, k < 2n  (DCT-IV)
 };
@@ -64,7 +67,7 @@ __global__ void __launch_bounds__(256) r2r_pre_kernel(const __grid_constant__ R2
   const T *in = reinterpret_cast<const T *>(a.in);
   cx<T> *ws = reinterpret_cast<cx<T> *>(a.out);
   const int n = a.n, M = a.M;
-  const T s2 = T(1.4142135623730951);
+  const T e0 = T(a.e0);
   for (int64_t g = blockIdx.y; g < a.nrows; g += gridDim.y) {
     const int64_t o = roff(a.ld, g);
     const int64_t s = a.ld.axis_stride;
@@ -75,7 +78,7 @@ __global__ void __launch_bounds__(256) r2r_pre_kernel(const __grid_constant__ R2
       if constexpr (K == K_DCT1) {
         const int src = j < n ? j : M - j;
         T val = x(src);
-        if (a.ortho && (src == 0 || src == n - 1)) val *= s2;
+        if (src == 0 || src == n - 1) val *= e0;
         v.x = val;
       } else if constexpr (K == K_DST1) {
         if (j >= 1 && j <= n) v.x = x(j - 1);
@@ -91,7 +94,7 @@ __global__ void __launch_bounds__(256) r2r_pre_kernel(const __grid_constant__ R2
         auto xpp = [&](int q) {
           const int src = a.cosine ? q : n - 1 - q;
           T val = x(src);
-          if (a.ortho && src == 0) val *= s2;
+          if (src == 0) val *= e0;
           return val;
         };
         const T re = xpp(j), im = j == 0 ? T(0) : -xpp(n - j);
@@ -131,7 +134,7 @@ __global__ void __launch_bounds__(256) r2r_post_kernel(const __grid_constant__ R
   T *out = reinterpret_cast<T *>(a.out);
   const int n = a.n, M = a.M;
   const T fct = T(a.fct);
-  const T h2 = T(0.7071067811865476);  // sqrt2 * 0.5
+  const T e0 = T(a.e0), e1 = T(a.e1);
   for (int64_t g = blockIdx.y; g < a.nrows; g += gridDim.y) {
     const int64_t o = roff(a.st, g);
     const int64_t s = a.st.axis_stride;
@@ -140,14 +143,14 @@ __global__ void __launch_bounds__(256) r2r_post_kernel(const __grid_constant__ R
       T y;
       if constexpr (K == K_DCT1) {
         y = W[k].x * fct;
-        if (a.ortho && (k == 0 || k == n - 1)) y *= h2;
+        if (k == 0 || k == n - 1) y *= e1;
       } else if constexpr (K == K_DST1) {
         y = -W[k + 1].y * fct;
       } else if constexpr (K == K_DCT2) {
         const int kk = a.cosine ? k : n - 1 - k;
         const cx<T> t = reinterpret_cast<const cx<T> *>(a.wa)[kk];
         y = T(2) * (W[kk].x * t.x - W[kk].y * t.y) * fct;
-        if (a.ortho && k == 0) y *= h2;
+        if (k == 0) y *= e0;
       } else if constexpr (K == K_DCT3) {
         const int j = (k & 1) ? n - 1 - (k >> 1) : (k >> 1);
         y = W[j].x * fct;
@@ -217,7 +220,7 @@ template <typename T> void launch_post(int K, const R2RArgs &a, cudaStream_t st)
 
 // One real-to-real axis job through a complex workspace.
 void r2r_axis(DType dt, int K, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
-              int64_t nrows, bool cosine, bool ortho, bool neg, double fct, cudaStream_t st) {
+              int64_t nrows, bool cosine, bool neg, double fct, double e0, double e1, cudaStream_t st) {
   int64_t M = n;
   if (K == K_DCT1) M = 2 * (n - 1);
   if (K == K_DST1) M = 2 * (n + 1);
@@ -234,9 +237,10 @@ void r2r_axis(DType dt, int K, int64_t n, const void *in, const Side &ld, void *
   a.n = int(n);
   a.M = int(M);
   a.cosine = cosine;
-  a.ortho = ortho;
   a.neg = neg;
   a.fct = fct;
+  a.e0 = e0;
+  a.e1 = e1;
   if (K == K_DCT2 || K == K_DCT3 || K == K_DCT4) a.wa = get_roots(uint64_t(4 * n), uint64_t(n), dt);
   if (K == K_DCT4) a.wb = get_roots(uint64_t(8 * n), uint64_t(2 * n), dt);
   if (dt == DType::F32)
@@ -312,10 +316,26 @@ template <typename T> __global__ void __launch_bounds__(256) hartley_gen_kernel(
 }  // namespace
 
 void exec_dcst(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, int type, bool cosine,
-               double fct, bool ortho, cudaStream_t st) {
-  const int K = type == 1 ? (cosine ? K_DCT1 : K_DST1) : type == 2 ? K_DCT2 : type == 3 ? K_DCT3 : K_DCT4;
+               double fct, bool ortho, cudaStream_t st, bool adjoint) {
+  const double r2 = 1.4142135623730951, h2 = 0.7071067811865476;
+  int K = type == 1 ? (cosine ? K_DCT1 : K_DST1) : type == 2 ? K_DCT2 : type == 3 ? K_DCT3 : K_DCT4;
+  // element weights of the reference's `ortho` (HDR:2931-2947, 3040-3045)
+  double e0 = 1, e1 = 1;
+  if (K == K_DCT1 && ortho) e0 = r2, e1 = h2;
+  if (K == K_DCT2 && ortho) e0 = h2;
+  if (K == K_DCT3 && ortho) e0 = r2;
+  if (adjoint) {
+    // transposes: DCT-II^T = DCT-III with input element 0 weighted 2 (sqrt2 with ortho);
+    // DCT-III^T = DCT-II with output element 0 weighted 1/2 (1/sqrt2 with ortho);
+    // DCT-I^T weights the input ends by 2 and the output ends by 1/2 (ortho DCT-I, DST-I and
+    // types 4 are their own transposes)
+    RG_CHECK(cosine || type == 1 || type == 4, RG_ERR_UNSUPPORTED, "adjoint of DST-II/III is not provided");
+    if (K == K_DCT2) K = K_DCT3, e0 = ortho ? r2 : 2.0;
+    else if (K == K_DCT3) K = K_DCT2, e0 = ortho ? h2 : 0.5;
+    else if (K == K_DCT1 && !ortho) e0 = 2.0, e1 = 0.5;
+  }
   real_nd(in, out, axes, fct, [&](int64_t n, const void *src, const Side &ld, void *dst, const Side &sd, int64_t rows,
-                                  double f) { r2r_axis(dt, K, n, src, ld, dst, sd, rows, cosine, ortho, false, f, st); });
+                                  double f) { r2r_axis(dt, K, n, src, ld, dst, sd, rows, cosine, false, f, e0, e1, st); });
 }
 
 void exec_r2r_fftpack(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool r2h, bool forward,
@@ -325,7 +345,7 @@ void exec_r2r_fftpack(DType dt, const NdArray &in, const NdArray &out, const Axe
   const int K = forward ? K_R2HC : K_HC2R;
   const bool neg = forward ? !r2h : r2h;
   real_nd(in, out, axes, fct, [&](int64_t n, const void *src, const Side &ld, void *dst, const Side &sd, int64_t rows,
-                                  double f) { r2r_axis(dt, K, n, src, ld, dst, sd, rows, true, false, neg, f, st); });
+                                  double f) { r2r_axis(dt, K, n, src, ld, dst, sd, rows, true, neg, f, 1, 1, st); });
 }
 
 void exec_hartley(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool genuine, double fct,
@@ -334,7 +354,7 @@ void exec_hartley(DType dt, const NdArray &in, const NdArray &out, const Axes &a
   if (!genuine || axes.size() == 1) {
     real_nd(in, out, axes, fct, [&](int64_t n, const void *src, const Side &ld, void *dst, const Side &sd,
                                     int64_t rows, double f) {
-      r2r_axis(dt, K_HARTLEY, n, src, ld, dst, sd, rows, true, false, false, f, st);
+      r2r_axis(dt, K_HARTLEY, n, src, ld, dst, sd, rows, true, false, f, 1, 1, st);
     });
     return;
   }

@@ -41,6 +41,9 @@ __all__ = [
     "r2r_separable_hartley",
     "r2r_genuine_hartley",
     "good_size",
+    "r2c_adjoint",
+    "c2r_adjoint",
+    "dct_adjoint",
     "set_stream",
     "plan_cache_entries",
     "plan_cache_bytes",
@@ -300,6 +303,25 @@ def r2r_separable_hartley(ain, aout, axes, fct, nthreads):
 def r2r_genuine_hartley(ain, aout, axes, fct, nthreads):
     """Genuine (non-separable) Hartley transform (``rocket_fft/_pocketfft_numba.cpp:205-223``)."""
     _hartley_call("numba_r2r_genuine_hartley_st", ain, aout, axes, fct, nthreads)
+
+
+def r2c_adjoint(ain, aout, axes, forward, fct, nthreads):
+    """Adjoint of ``r2c(., ., axes, forward, fct)``: ``ain`` is the half-spectrum cotangent,
+    ``aout`` (real) receives the input cotangent. A c2r in the opposite direction with the
+    interior bins of the last axis halved (the Hermitian bin weighting)."""
+    _cmplx_call("rocketgpu_r2c_adjoint_st", ain, aout, axes, forward, fct, nthreads)
+
+
+def c2r_adjoint(ain, aout, axes, forward, fct, nthreads):
+    """Adjoint of ``c2r(., ., axes, forward, fct)``: ``ain`` is the real cotangent, ``aout``
+    receives the half-spectrum cotangent (an r2c in the opposite direction, interior bins of the
+    last axis doubled)."""
+    _cmplx_call("rocketgpu_c2r_adjoint_st", ain, aout, axes, forward, fct, nthreads)
+
+
+def dct_adjoint(ain, aout, axes, type, fct, ortho, nthreads):
+    """Transpose of ``dct(., ., axes, type, fct, ortho)``."""
+    _real_call("rocketgpu_dct_adjoint_st", ain, aout, axes, type, fct, ortho, nthreads)
 
 
 def good_size(n, real):
