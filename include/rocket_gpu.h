@@ -127,6 +127,24 @@ int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, ro
                              rocketgpu_arystruct_t *axes, uint64_t type, double fct, bool ortho,
                              uint64_t nthreads);
 
+/* ---- spectral Poisson solver kernels (no reference counterpart; the DCT-II/III application of
+ * the transform path). Grids are C-contiguous n0 x n1 x n2, h = 1, Neumann boundaries (mirrored
+ * ghost cells); the DCT-II diagonalises the 7-point Laplacian with eigenvalues
+ * lam0[k0] + lam1[k1] + lam2[k2], lam_a[k] = 2 cos(pi k / n_a) - 2.
+ *   rocketgpu_poisson_eigdiv: X /= lambda in place (float or double, itemsize 4/8), mode 0 set
+ *     to 0; lam = the three device tables back to back (n0+n1+n2 doubles).
+ *   rocketgpu_poisson_update: u += delta with an exact two-sum whose rounding error goes to the
+ *     float u_lo (u_lo may be NULL).
+ *   rocketgpu_poisson_residual: r = f - A (u + u_lo) in double (u_lo may be NULL), written as
+ *     float to r32 (if not NULL); sum(r^2) to *sumsq (device).
+ * All return a status; rocketgpu_poisson_last_error gives the calling thread's message. */
+int rocketgpu_poisson_eigdiv(void *X, int64_t itemsize, int64_t n0, int64_t n1, int64_t n2, const double *lam,
+                             void *stream);
+int rocketgpu_poisson_update(double *u, float *u_lo, const float *delta, int64_t total, void *stream);
+int rocketgpu_poisson_residual(const double *u, const float *u_lo, const double *f, float *r32, int64_t n0,
+                               int64_t n1, int64_t n2, double *sumsq, void *stream);
+const char *rocketgpu_poisson_last_error(void);
+
 /* ---- runtime control (no reference counterpart) ---- */
 
 /* Status and message of the calling thread's most recent call (RG_OK / "" after success).

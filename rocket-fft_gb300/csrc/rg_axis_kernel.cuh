@@ -115,7 +115,20 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
           if (r < rows) {
             rr[u] = r;
             ii[u] = i;
-            v[u] = load_unit<T, OP>(a.in, roff_in[r], i, s);
+            if constexpr (OP == OP_DCT2) {
+              v[u] = mk<T>(__ldg(reinterpret_cast<const T *>(a.in) + roff_in[r] + i * s), T(0));
+            } else if constexpr (OP == OP_DCT3) {
+              // (x''_i, x''_{n-i}) with x''_q = x_q (DCT) or x_{n-1-q} (DST); x''_n = 0
+              const T *in = reinterpret_cast<const T *>(a.in) + roff_in[r];
+              const int n = a.n;
+              const bool sine = (a.flags & 2) != 0;
+              const int sa = sine ? n - 1 - i : i;
+              const T xa = __ldg(in + sa * s);
+              const T xb = i == 0 ? T(0) : __ldg(in + (sine ? i - 1 : n - i) * s);
+              v[u] = mk<T>(xa, xb);
+            } else {
+              v[u] = load_unit<T, OP>(a.in, roff_in[r], i, s);
+            }
           }
         }
       }
@@ -139,6 +152,21 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
           if (i == 0 || i == L) x.y = T(0);
           else x = scl<T>(x, bsc);
           sm[sidx(r, i, pitch, ps)] = x;
+        } else if constexpr (OP == OP_DCT2) {
+          // Makhoul order: x_2j -> j, x_2j+1 -> n-1-j; DST: odd inputs negated
+          const int n = a.n;
+          const int j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
+          if ((a.flags & 2) && (i & 1)) x.x = -x.x;
+          sm[sidx(r, j, pitch, ps)] = x;
+        } else if constexpr (OP == OP_DCT3) {
+          // conj(V_i), V_i = (x''_i - i x''_{n-i}) e^{i pi i / 2n}; input element 0 weighted e0
+          const int n = a.n;
+          const bool sine = (a.flags & 2) != 0;
+          const T e0 = T(a.e0);
+          if (sine ? i == n - 1 : i == 0) x.x *= e0;
+          if (sine && i == 1) x.y *= e0;
+          const cx<T> t = reinterpret_cast<const cx<T> *>(a.aux)[i];  // e^{-i pi i / 2n}
+          sm[sidx(r, i, pitch, ps)] = cj<T>(mulc<T>(mk<T>(x.x, -x.y), t));
         } else if constexpr (OP == OP_C2R_ODD) {
           // units = (n+1)/2 bins; build conj of the full Hermitian spectrum:
           //   W_0 = Re X_0, W_i = conj(X_i), W_{n-i} = X_i
@@ -253,6 +281,25 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
           if (r < rows) {
             rr[u] = r;
             ii[u] = i;
+            if constexpr (OP == OP_DCT2) {
+              // y_k = 2 Re(e^{-i pi k'/2n} V_k'), k' = k (DCT) or n-1-k (DST); element 0 weighted
+              const int n = a.n;
+              const int kk = (a.flags & 2) ? n - 1 - i : i;
+              const cx<T> V = res[sidx(r, kk, pitch, ps)];
+              const cx<T> t = reinterpret_cast<const cx<T> *>(a.aux)[kk];
+              T y = T(2) * (V.x * t.x - V.y * t.y) * fct;
+              if (i == 0) y *= T(a.e0);
+              v[u] = mk<T>(y, T(0));
+              continue;
+            } else if constexpr (OP == OP_DCT3) {
+              // y_2j = Re v_j, y_2j+1 = Re v_{n-1-j}; DST: odd outputs negated
+              const int n = a.n;
+              const int j = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
+              T y = res[sidx(r, j, pitch, ps)].x * fct;
+              if ((a.flags & 2) && (i & 1)) y = -y;
+              v[u] = mk<T>(y, T(0));
+              continue;
+            }
             cx<T> x = res[sidx(r, i, pitch, ps)];
             if constexpr (OP == OP_C2C_TW) {
               x = mul<T>(x, split_twiddle<T>(reinterpret_cast<const cx<T> *>(a.aux),
@@ -290,7 +337,7 @@ __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs
             out[off + 2 * i * s] = v[u].x;
             out[off + (2 * i + 1) * s] = v[u].y;
           }
-        } else if constexpr (OP == OP_C2R_ODD) {
+        } else if constexpr (OP == OP_C2R_ODD || OP == OP_DCT2 || OP == OP_DCT3) {
           reinterpret_cast<T *>(a.out)[off + i * s] = v[u].x;
         } else {
           reinterpret_cast<cx<T> *>(a.out)[off + i * s] = v[u];

@@ -90,10 +90,11 @@ struct KArgs {
   int ps;          // pad shift: shared index i is stored at i + (i >> ps)
   int conj_in;     // conjugate while loading (backward transforms run the forward core on
   int conj_out;    // conjugated data) / while storing
-  int flags;       // op-specific (cosine/ortho/type bits, ...)
+  int flags;       // op-specific: bit 1 = sine transform (DST) for the fused DCT ops
   double fct;      // scale applied to every output
   double bscale;   // r2c/c2r: extra scale of the interior half-spectrum bins 0 < k < n/2 (1 for
                    // the transforms; 2 / 0.5 for the adjoints of c2r / r2c)
+  double e0;       // fused DCT-II: weight of output element 0; DCT-III: of input element 0
   const void *aux;   // op-specific table (split twiddles, chirp, ...)
   const void *aux2;  // op-specific second table (Bluestein spectrum, ...)
   int aux_n;         // op-specific integer (four-step: number of columns)

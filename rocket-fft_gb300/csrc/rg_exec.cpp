@@ -177,7 +177,8 @@ Geo choose_geo(DType dt, int L, int Lsm, bool col, int64_t nrows, bool pow2tb) {
   if (int64_t(TB) > nrows && !(pow2tb && col)) TB = int(std::max<int64_t>(1, nrows));
   if (pow2tb)
     while (TB & (TB - 1)) TB &= TB - 1;
-  const size_t budget_soft = col ? 160 * 1024 : 112 * 1024;
+  // at most ~80 KB per CTA so that at least two CTAs share an SM
+  const size_t budget_soft = 80 * 1024;
   for (;;) {
     const size_t smem = smem_bytes(dt, TB, g.pitch);
     if (smem <= (TB == 1 ? maxsm : std::min(maxsm, budget_soft))) {
@@ -202,23 +203,7 @@ bool pow2_enabled() {
   return on;
 }
 
-struct Job {
-  DType dt;
-  int op;
-  int n;     // logical length
-  int L;     // core length
-  int Lsm;   // shared slots per row
-  int nin, nout;
-  const void *in;
-  void *out;
-  Side ld, st;
-  int64_t nrows;
-  bool cin, cout;
-  double fct;
-  const void *aux = nullptr, *aux2 = nullptr;
-  int aux_n = 1, aux_s = 0;
-  double bscale = 1.0;  // interior half-spectrum bin scale (r2c/c2r adjoints)
-};
+
 
 void run_job(const Job &j, cudaStream_t st) {
   if (j.nrows <= 0) return;
@@ -252,6 +237,8 @@ void run_job(const Job &j, cudaStream_t st) {
   a.aux_n = j.aux_n;
   a.aux_s = j.aux_s;
   a.bscale = j.bscale;
+  a.e0 = j.e0;
+  a.flags = j.flags;
   a.core = ct.core;
   const size_t smem = g.smem;
   LaunchCfg cfg;

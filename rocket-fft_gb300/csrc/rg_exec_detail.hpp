@@ -26,6 +26,28 @@ Side contiguous_rows(int64_t nrows, int64_t len);
 bool fits_core(int64_t L, DType dt);
 bool any_zero(const std::vector<int64_t> &shape);
 
+// One on-chip axis job (a single kernel launch).
+struct Job {
+  DType dt;
+  int op;
+  int n;     // logical length
+  int L;     // core length
+  int Lsm;   // shared slots per row
+  int nin, nout;
+  const void *in;
+  void *out;
+  Side ld, st;
+  int64_t nrows;
+  bool cin, cout;
+  double fct;
+  const void *aux = nullptr, *aux2 = nullptr;
+  int aux_n = 1, aux_s = 0;
+  double bscale = 1.0;  // interior half-spectrum bin scale (r2c/c2r adjoints)
+  double e0 = 1.0;      // fused DCT ops: element-0 weight
+  int flags = 0;        // fused DCT ops: bit 1 = DST
+};
+void run_job(const Job &j, cudaStream_t st);
+
 // Complex transforms of `nrows` rows of length n (any n: on chip, four-step or Bluestein),
 // the forward core on data conjugated on load (cin) and store (cout), scaled by fct.
 void c2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,

@@ -55,6 +55,8 @@ template <typename T> void launch_axis_typed(int op, const KArgs &a, const Launc
     case OP_C2R_EVEN: launch_axis_t<T, OP_C2R_EVEN>(a, cfg, st); break;
     case OP_C2R_ODD: launch_axis_t<T, OP_C2R_ODD>(a, cfg, st); break;
     case OP_BLUE: launch_axis_t<T, OP_BLUE>(a, cfg, st); break;
+    case OP_DCT2: launch_axis_t<T, OP_DCT2>(a, cfg, st); break;
+    case OP_DCT3: launch_axis_t<T, OP_DCT3>(a, cfg, st); break;
     default: throw Error(RG_ERR_INTERNAL, "launch_axis: unknown op");
   }
 }

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 
 #include "rg_error.hpp"
 #include "rg_exec.hpp"
@@ -218,6 +219,16 @@ template <typename T> void launch_post(int K, const R2RArgs &a, cudaStream_t st)
   RG_CUDA(cudaGetLastError());
 }
 
+// Fused DCT-II/III kernels can be switched off (ROCKET_GPU_FUSED_DCT=0) to compare against the
+// three-kernel route.
+bool fused_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("ROCKET_GPU_FUSED_DCT");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 // One real-to-real axis job through a complex workspace.
 void r2r_axis(DType dt, int K, int64_t n, const void *in, const Side &ld, void *out, const Side &sd,
               int64_t nrows, bool cosine, bool neg, double fct, double e0, double e1, cudaStream_t st) {
@@ -227,6 +238,25 @@ void r2r_axis(DType dt, int K, int64_t n, const void *in, const Side &ld, void *
   if (K == K_DCT4) M = 2 * n;
   RG_CHECK(M >= 1, RG_ERR_ARG, "zero-length FFT requested");
   RG_CHECK(M < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
+  if ((K == K_DCT2 || K == K_DCT3) && fused_enabled() && detail::fits_core(n, dt)) {
+    // one kernel: the reordering / twiddles of the reduction fused into the on-chip FFT's load
+    // and store phases
+    detail::Job j{};
+    j.dt = dt;
+    j.op = K == K_DCT2 ? OP_DCT2 : OP_DCT3;
+    j.n = j.L = j.Lsm = j.nin = j.nout = int(n);
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.fct = fct;
+    j.e0 = e0;
+    j.flags = cosine ? 0 : 2;
+    j.aux = get_roots(uint64_t(4 * n), uint64_t(n), dt);
+    detail::run_job(j, st);
+    return;
+  }
   DevBuf ws(size_t(nrows) * size_t(M) * cx_size(dt), st);
   R2RArgs a{};
   a.in = in;

@@ -59,15 +59,16 @@ def test_golden_replay(rg, golden, cuda, where):
 
 
 def test_golden_replay_generic_kernel_only(tmp_path):
-    """The same replay with the power-of-two kernel switched off (ROCKET_GPU_POW2=0), so the
-    generic kernel stays covered for lengths the specialised one normally takes."""
+    """The same replay with the power-of-two kernel and the fused DCT-II/III kernels switched off
+    (ROCKET_GPU_POW2=0, ROCKET_GPU_FUSED_DCT=0), so the generic kernel and the three-kernel DCT
+    route stay covered for lengths the specialised ones normally take."""
     import os
     import subprocess
     import sys
 
     from conftest import ROOT
 
-    env = dict(os.environ, ROCKET_GPU_POW2="0")
+    env = dict(os.environ, ROCKET_GPU_POW2="0", ROCKET_GPU_FUSED_DCT="0")
     r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-m", "gpu",
                         str(ROOT / "tests" / "test_gpu_golden.py") + "::test_golden_replay"],
                        env=env, capture_output=True, text=True, cwd=str(ROOT))
