@@ -145,6 +145,21 @@ int rocketgpu_poisson_residual(const double *u, const float *u_lo, const double 
                                int64_t n1, int64_t n2, double *sumsq, void *stream);
 const char *rocketgpu_poisson_last_error(void);
 
+/* ---- batched uneven-length complex FFTs (no reference counterpart) ----
+ * One plan for `count` transforms of the given lengths (complex64: itemsize 8, complex128: 16),
+ * all forward or all backward, scaled by fct. Rows are stored back to back in flat device
+ * buffers (row i starts at sum of lengths[0..i-1]). Execution is one persistent kernel launch
+ * (plus a 4-byte counter reset) that allocates nothing, so it can be captured in a CUDA graph.
+ * With autotune, rocketgpu_batch_create times the candidate schedules (on-chip capacity per CTA,
+ * threads per CTA, four-step split policy) on these lengths and keeps the fastest;
+ * rocketgpu_batch_info returns the choice and the timings as JSON. create returns NULL on error
+ * (rocketgpu_last_error has the message). */
+void *rocketgpu_batch_create(const int64_t *lengths, int64_t count, int64_t itemsize, bool forward, double fct,
+                             int autotune);
+int rocketgpu_batch_exec(void *plan, const void *in, void *out, void *stream);
+int rocketgpu_batch_info(void *plan, char *buf, size_t len);
+void rocketgpu_batch_destroy(void *plan);
+
 /* ---- runtime control (no reference counterpart) ---- */
 
 /* Status and message of the calling thread's most recent call (RG_OK / "" after success).

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/rocket_gpu.h"
+#include "rg_batch.hpp"
 #include "rg_error.hpp"
 #include "rg_exec.hpp"
 #include "rg_launch.hpp"
@@ -419,6 +420,47 @@ RG_EXPORT int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_
                                        rocketgpu_arystruct_t *aout, rocketgpu_arystruct_t *axes, uint64_t type,
                                        double fct, bool ortho, uint64_t) {
   return do_dcst(ndim, ain, aout, axes, type, fct, ortho, true, true);
+}
+
+// ---------------------------------------------------------------------------------------
+// batched uneven lengths (no reference counterpart)
+// ---------------------------------------------------------------------------------------
+
+RG_EXPORT void *rocketgpu_batch_create(const int64_t *lengths, int64_t count, int64_t itemsize, bool forward,
+                                       double fct, int autotune) {
+  rg::BatchPlan *p = nullptr;
+  guarded([&] {
+    RG_CHECK(lengths != nullptr, RG_ERR_ARG, "lengths is NULL");
+    const DType dt = complex_dtype(itemsize);
+    p = rg::batch_create(lengths, count, dt, forward, fct, autotune != 0);
+  });
+  return p;
+}
+
+RG_EXPORT int rocketgpu_batch_exec(void *plan, const void *in, void *out, void *stream) {
+  return guarded([&] {
+    RG_CHECK(plan != nullptr, RG_ERR_ARG, "plan is NULL");
+    RG_CHECK(is_device_ptr(in) && is_device_ptr(out), RG_ERR_UNSUPPORTED, "batch buffers must be device memory");
+    rg::batch_exec(*static_cast<rg::BatchPlan *>(plan), in, out, static_cast<cudaStream_t>(stream));
+  });
+}
+
+RG_EXPORT int rocketgpu_batch_info(void *plan, char *buf, size_t len) {
+  std::string info;
+  const int st = guarded([&] {
+    RG_CHECK(plan != nullptr, RG_ERR_ARG, "plan is NULL");
+    info = rg::batch_info(*static_cast<rg::BatchPlan *>(plan));
+  });
+  if (buf && len > 0) {
+    const size_t n = std::min(len - 1, info.size());
+    std::memcpy(buf, info.data(), n);
+    buf[n] = '\0';
+  }
+  return st;
+}
+
+RG_EXPORT void rocketgpu_batch_destroy(void *plan) {
+  guarded([&] { rg::batch_destroy(static_cast<rg::BatchPlan *>(plan)); });
 }
 
 // ---------------------------------------------------------------------------------------
