@@ -61,6 +61,8 @@ struct Side {
   int64_t bstride[kMaxBatchDims];
   int nbd;
   int colmap;  // 1: consecutive threads walk consecutive rows (rows are adjacent in memory)
+  FastDiv bdiv[kMaxBatchDims];  // reciprocals of bshape (set by the launcher for kernels that
+                                // decompose 32-bit row numbers, rg_fixed_kernel.cuh)
 };
 
 // What the kernel does around the on-chip FFT.

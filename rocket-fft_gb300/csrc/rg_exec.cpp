@@ -205,6 +205,67 @@ bool pow2_enabled() {
 
 
 
+// The persistent pipelined kernel (rg_stream_kernel.cuh) can be switched off
+// (ROCKET_GPU_STREAM=0); ROCKET_GPU_STREAM_S picks its stage count (2..4, default 2).
+bool stream_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("ROCKET_GPU_STREAM");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+// The compile-time-L kernels (rg_fixed_kernel.cuh) can be switched off (ROCKET_GPU_FIXED=0).
+bool fixed_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("ROCKET_GPU_FIXED");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+// Reciprocals of the batch extents for 32-bit row decomposition; false if an extent does not
+// fit the reciprocal range.
+bool set_fastdivs(Side &s) {
+  for (int d = 0; d < s.nbd; ++d) {
+    if (s.bshape[d] <= 0 || s.bshape[d] >= (int64_t(1) << 31)) return false;
+    s.bdiv[d] = make_fastdiv(uint32_t(s.bshape[d]));
+  }
+  return true;
+}
+int stream_stages() {
+  static const int s = [] {
+    const char *e = std::getenv("ROCKET_GPU_STREAM_S");
+    const int v = e ? std::atoi(e) : 2;
+    return v < 2 ? 2 : v > 4 ? 4 : v;
+  }();
+  return s;
+}
+
+// Geometry of the pipelined kernel: tiles of about 32 KB (4096 complex64 / 2048 complex128
+// elements), 16 (8) rows for a column walk so that a tile row is one 128-byte segment, one
+// radix-16 butterfly per thread, stages + 1 tile buffers and S + 1 slots of row offsets.
+// Returns false when no tile fits in shared memory.
+bool stream_geo(const Job &j, bool col, int stages, Geo &g) {
+  const int esz = int(cx_size(j.dt));
+  g.pitch = row_pitch(j.dt, j.Lsm, g.ps);
+  const int target = j.dt == DType::F32 ? 4096 : 2048;
+  int TB = col ? (j.dt == DType::F32 ? 16 : 8) : std::max(1, target / j.L);
+  while (TB & (TB - 1)) TB &= TB - 1;
+  const size_t maxsm = max_smem_optin();
+  for (;;) {
+    const size_t smem = size_t(stages + 1) * TB * g.pitch * esz + size_t(stages + 1) * 2 * TB * 8;
+    if (smem <= maxsm) {
+      g.TB = TB;
+      g.smem = smem;
+      const int64_t bf = int64_t(TB) * j.L / 16;
+      g.threads = int(std::min<int64_t>(512, std::max<int64_t>(64, (bf + 31) / 32 * 32)));
+      return true;
+    }
+    if (TB == 1 || (col && TB <= 4)) return false;
+    TB /= 2;
+  }
+}
+
 void run_job(const Job &j, cudaStream_t st) {
   if (j.nrows <= 0) return;
   const CoreTables &ct = get_core(j.L, j.dt);
@@ -216,7 +277,26 @@ void run_job(const Job &j, cudaStream_t st) {
   const bool pow2_op = j.op == OP_C2C || j.op == OP_C2C_TW || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN;
   const bool pow2 = pow2_op && j.L >= 2 && (j.L & (j.L - 1)) == 0 && pow2_enabled() &&
                     !((j.op == OP_C2C || j.op == OP_C2C_TW) && ct.core.npass == 1 && ld.colmap != sd.colmap);
-  const Geo g = choose_geo(j.dt, j.L, j.Lsm, ld.colmap || sd.colmap, j.nrows, pow2);
+  // pipelined kernel: element-aligned sources (cp.async copies whole complex units)
+  const size_t csz = cx_size(j.dt);
+  bool stream = pow2 && stream_enabled() && (j.op == OP_C2C || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN) &&
+                j.L >= 16;
+  int pair_ok = 0;
+  if (stream) {
+    const uintptr_t base = reinterpret_cast<uintptr_t>(j.in);
+    if (j.op == OP_R2C_EVEN) {
+      bool even = ld.axis_stride == 1 && base % csz == 0;
+      for (int d = 0; d < ld.nbd; ++d) even = even && (ld.bstride[d] % 2 == 0);
+      pair_ok = even ? 1 : 0;
+      stream = base % real_size(j.dt) == 0;
+    } else {
+      stream = base % csz == 0;
+    }
+  }
+  Geo g{};
+  const int stages = stream_stages();
+  if (stream) stream = stream_geo(j, ld.colmap != 0, stages, g);
+  if (!stream) g = choose_geo(j.dt, j.L, j.Lsm, ld.colmap || sd.colmap, j.nrows, pow2);
   KArgs a{};
   a.in = j.in;
   a.out = j.out;
@@ -248,6 +328,29 @@ void run_job(const Job &j, cudaStream_t st) {
   cfg.threads = g.threads;
   cfg.smem = smem;
   cfg.pow2 = pow2;
+  if (stream) {
+    cfg.stages = stages;
+    cfg.pair_ok = pair_ok;
+  }
+  // compile-time-L kernel: power-of-two L, both sides walking alike, 32-bit row numbers,
+  // C2C conjugating on both sides or neither
+  if (pow2 && !stream && fixed_enabled() && (j.op == OP_C2C || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN) &&
+      ld.colmap == sd.colmap && j.nrows < (int64_t(1) << 31) && (j.op != OP_C2C || j.cin == j.cout) &&
+      set_fastdivs(a.ld) && set_fastdivs(a.st)) {
+    cfg.fixed = true;
+    cfg.col = ld.colmap != 0;
+    cfg.bwd = j.op == OP_C2C && j.cin;
+    const size_t rsz = real_size(j.dt);
+    if (j.op == OP_R2C_EVEN) {
+      bool ok = ld.axis_stride == 1 && reinterpret_cast<uintptr_t>(j.in) % (2 * rsz) == 0;
+      for (int d = 0; d < ld.nbd; ++d) ok = ok && ld.bstride[d] % 2 == 0;
+      cfg.pair_ok = ok ? 1 : 0;
+    } else if (j.op == OP_C2R_EVEN) {
+      bool ok = sd.axis_stride == 1 && reinterpret_cast<uintptr_t>(j.out) % (2 * rsz) == 0;
+      for (int d = 0; d < sd.nbd; ++d) ok = ok && sd.bstride[d] % 2 == 0;
+      cfg.pair_ok = ok ? 1 : 0;
+    }
+  }
   launch_axis(j.dt, j.op, a, cfg, st);
 }
 

@@ -1,0 +1,400 @@
+// Axis-job kernel compiled for one power-of-two core length L = 2^E.
+//
+// The runtime-parameterised kernels (rg_axis_kernel.cuh, rg_pow2_kernel.cuh) carry every
+// radix and pass shape in one binary and compute shared-memory and twiddle indices at run
+// time; on GB300 they are bound by instruction issue (integer index arithmetic and
+// instruction-cache misses), not by HBM. Here the pass schedule (the same radices as the host
+// core plan, core_radices in rg_plan.cpp), the rows per CTA (TB), the thread count, the
+// shared-memory pitch and every per-pass index are compile-time constants, so a butterfly's
+// shared and twiddle accesses are immediate offsets from one base address and the kernel
+// holds only the code of its own passes.
+//
+// Walks: COL = rows are adjacent columns of a strided axis (threads run across rows, TB rows
+// give one 128-byte segment per position); ROW = rows are contiguous along the axis (threads
+// run along the row). Both sides of the job walk the same way.
+//
+// Flows (pass 0 reads global memory directly, the last pass of C2C / C2R_EVEN writes it; one
+// shared buffer A per CTA, passes in between run in place: all reads, barrier, all writes):
+//   C2C       global -> A [-> A ...] -> global; backward = the forward core applied to
+//             (im, re)-swapped data, swapped back on store (swap(F(swap(x))) = conj(F(conj(x))))
+//   R2C_EVEN  real pairs -> A -> ... (all passes on chip), split into X_0..X_L, staged store
+//   C2R_EVEN  staged Hermitian load, merge into conj(Z), passes, real pairs to global
+#pragma once
+#include "rg_axis_kernel.cuh"
+
+namespace rg {
+namespace fx {
+
+// radices of a power-of-two core 2^e, identical to core_radices(): 16^a, then 2/4/8, with
+// 16^(a-1) * 8 * 4 instead of 16^a * 2
+__host__ __device__ constexpr int np_of(int e) {
+  return (e % 4 == 1 && e / 4 >= 1) ? e / 4 + 1 : e / 4 + (e % 4 ? 1 : 0);
+}
+__host__ __device__ constexpr int radix_of(int e, int p) {
+  return (e % 4 == 1 && e / 4 >= 1) ? (p < e / 4 - 1 ? 16 : p == e / 4 - 1 ? 8 : 4)
+         : (p < e / 4 ? 16 : e % 4 == 1 ? 2 : e % 4 == 2 ? 4 : 8);
+}
+__host__ __device__ constexpr int ns_of(int e, int p) {
+  int n = 1;
+  for (int q = 0; q < p; ++q) n *= radix_of(e, q);
+  return n;
+}
+// offset of pass p's twiddles in the core table; the table has no entries for pass 0 (Ns = 1)
+__host__ __device__ constexpr int tw_of(int e, int p) {
+  int t = 0;
+  for (int q = 1; q < p; ++q) t += (radix_of(e, q) - 1) * ns_of(e, q);
+  return t;
+}
+// padded row pitch (as row_pitch() on the host): index i at i + (i >> ps), pitch = 1 mod the
+// number of elements per 128-byte bank line
+__host__ __device__ constexpr int pitch_of(int lsm, int ps, int esz) {
+  int p = lsm + ((lsm - 1) >> ps) + 1;
+  while (p % (128 / esz) != 1) ++p;
+  return p;
+}
+__host__ __device__ constexpr int clampi(int x, int lo, int hi) { return x < lo ? lo : x > hi ? hi : x; }
+
+}  // namespace fx
+
+template <typename T, int OP, int E, bool COL> struct FxCfg {
+  static constexpr int L = 1 << E;
+  static constexpr int NP = fx::np_of(E);
+  static constexpr int ESZ = int(2 * sizeof(T));
+  static constexpr int PS = sizeof(T) == 4 ? 4 : 3;
+  static constexpr int LSM = OP == OP_C2C ? L : L + 1;
+  static constexpr int PITCH = fx::pitch_of(LSM, PS, ESZ);
+  static constexpr int TB = COL ? (sizeof(T) == 4 ? (L <= 256 ? 16 : 8) : (L <= 256 ? 8 : 4))
+                                : ((sizeof(T) == 4 ? 4096 : 2048) / L > 1 ? (sizeof(T) == 4 ? 4096 : 2048) / L : 1);
+  static constexpr int NT = fx::clampi(TB * L / 16, 64, 512);
+  static constexpr int NBUF = OP == OP_C2C && NP == 1 ? 0 : 1;  // middle passes run in place
+  static constexpr size_t SMEM = size_t(NBUF) * TB * PITCH * ESZ;
+  static_assert(NT % TB == 0 && NT / TB >= 1, "threads per row");
+};
+
+// Row offset of row g (< 2^32) through 32-bit reciprocal divisions.
+__device__ __forceinline__ int64_t side_offset32(const Side &s, uint32_t g) {
+  int64_t off = 0;
+  for (int d = 0; d < s.nbd; ++d) {
+    const uint32_t q = d + 1 < s.nbd ? fdiv(g, s.bdiv[d]) : 0u;
+    off += int64_t(g - q * uint32_t(s.bshape[d])) * s.bstride[d];
+    g = q;
+  }
+  return off;
+}
+
+// Padded shared position of element i = j + k * STEP (k compile-time): linear in k whenever
+// STEP is a multiple of the pad period.
+template <int PS, int STEP> __device__ __forceinline__ int fx_pos(int j, int k) {
+  if constexpr (STEP % (1 << PS) == 0) {
+    return j + (j >> PS) + k * (STEP + (STEP >> PS));
+  } else {
+    const int i = j + k * STEP;
+    return i + (i >> PS);
+  }
+}
+
+enum : int { FX_SMEM = 0, FX_GLOBAL = 1 };
+
+// Butterfly bf of pass p: its row and position.
+template <int TB, int LR, bool COL> __device__ __forceinline__ void fx_rj(int bf, int &r, int &j) {
+  if constexpr (COL) {
+    r = bf & (TB - 1);
+    j = bf / TB;
+  } else {
+    r = bf / LR;
+    j = bf & (LR - 1);
+  }
+}
+
+// Inputs of butterfly (r, j) of pass p: gathered from global memory (pass 0) or shared memory,
+// twiddled and transformed in registers.
+template <typename T, int OP, int E, int P, bool COL, bool BWD, int SRC>
+__device__ __forceinline__ void fx_compute(const KArgs &a, uint32_t row0, int r, int j, const cx<T> *__restrict__ src,
+                                           const cx<T> *__restrict__ tw, bool pair_ok,
+                                           cx<T> (&v)[fx::radix_of(E, P)]) {
+  using C = FxCfg<T, OP, E, COL>;
+  constexpr int L = C::L, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P), TWO = fx::tw_of(E, P);
+  constexpr int PS = C::PS, PITCH = C::PITCH;
+  if constexpr (SRC == FX_GLOBAL) {
+    const int64_t s = a.ld.axis_stride;
+    const int64_t off = side_offset32(a.ld, row0 + uint32_t(r));
+    if constexpr (OP == OP_R2C_EVEN) {
+      const T *in = reinterpret_cast<const T *>(a.in) + off;
+      if (pair_ok) {
+        const cx<T> *p = reinterpret_cast<const cx<T> *>(in) + j;
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = __ldg(p + k * LR);
+      } else {
+        const T *p = in + 2 * int64_t(j) * s;
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = mk<T>(__ldg(p + 2 * k * LR * s), __ldg(p + (2 * k * LR + 1) * s));
+      }
+    } else {
+      const cx<T> *p = reinterpret_cast<const cx<T> *>(a.in) + off + int64_t(j) * s;
+      const int64_t step = int64_t(LR) * s;
+#pragma unroll
+      for (int k = 0; k < R; ++k) v[k] = __ldg(p + k * step);
+      if constexpr (BWD) {
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = mk<T>(v[k].y, v[k].x);
+      }
+    }
+  } else {
+    const cx<T> *sp = src + r * PITCH;
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = sp[fx_pos<PS, LR>(j, k)];
+  }
+  if constexpr (NS > 1) {
+    const cx<T> *t = tw + TWO + (j & (NS - 1));
+#pragma unroll
+    for (int k = 1; k < R; ++k) v[k] = mul<T>(v[k], __ldg(t + (k - 1) * NS));
+  }
+  dft<T, R>(v);
+}
+
+// Outputs of butterfly (r, j) of pass p: to shared memory, or (last pass of C2C / C2R_EVEN)
+// to global memory with the op's output conversion.
+template <typename T, int OP, int E, int P, bool COL, bool BWD, int DST>
+__device__ __forceinline__ void fx_emit(const KArgs &a, uint32_t row0, int r, int j, cx<T> *__restrict__ dst,
+                                        bool scale, bool pair_ok, const cx<T> (&v)[fx::radix_of(E, P)]) {
+  using C = FxCfg<T, OP, E, COL>;
+  constexpr int R = fx::radix_of(E, P), NS = fx::ns_of(E, P);
+  constexpr int PS = C::PS, PITCH = C::PITCH;
+  const int m = j & (NS - 1);
+  const int base = (j - m) * R + m;
+  if constexpr (DST == FX_GLOBAL) {
+    const int64_t s = a.st.axis_stride;
+    const int64_t off = side_offset32(a.st, row0 + uint32_t(r));
+    const T fct = T(a.fct);
+    if constexpr (OP == OP_C2R_EVEN) {
+      // (x_2i, x_2i+1) = (Re F_i, -Im F_i) * fct
+      T *out = reinterpret_cast<T *>(a.out) + off;
+      if (pair_ok) {
+        cx<T> *p = reinterpret_cast<cx<T> *>(out) + base;
+#pragma unroll
+        for (int k = 0; k < R; ++k) p[k * NS] = scale ? mk<T>(v[k].x * fct, -v[k].y * fct) : mk<T>(v[k].x, -v[k].y);
+      } else {
+        T *p = out + 2 * int64_t(base) * s;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+          p[2 * k * NS * s] = v[k].x * fct;
+          p[(2 * k * NS + 1) * s] = -v[k].y * fct;
+        }
+      }
+    } else {
+      cx<T> *p = reinterpret_cast<cx<T> *>(a.out) + off + int64_t(base) * s;
+      const int64_t step = int64_t(NS) * s;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        cx<T> x = BWD ? mk<T>(v[k].y, v[k].x) : v[k];
+        if (scale) x = scl<T>(x, fct);
+        p[k * step] = x;
+      }
+    }
+  } else {
+    cx<T> *dp = dst + r * PITCH;
+    if constexpr (NS % (1 << PS) == 0) {
+      const int b0 = base + (base >> PS);
+#pragma unroll
+      for (int k = 0; k < R; ++k) dp[b0 + k * (NS + (NS >> PS))] = v[k];
+    } else if constexpr (NS == 1 && ((1 << PS) % R) == 0) {
+      const int b0 = base + (base >> PS);  // base = R * j: the R outputs share one pad block
+#pragma unroll
+      for (int k = 0; k < R; ++k) dp[b0 + k] = v[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int i = base + k * NS;
+        dp[i + (i >> PS)] = v[k];
+      }
+    }
+  }
+}
+
+// One radix pass p of the compile-time schedule. Rows r >= rows (tail tile) are skipped.
+// INPL: source and destination are the same shared buffer; every butterfly of the CTA reads
+// its inputs (and transforms them) before a barrier, then all write.
+template <typename T, int OP, int E, int P, bool COL, bool BWD, int SRC, int DST, bool INPL = false>
+__device__ __forceinline__ void fx_pass(const KArgs &a, uint32_t row0, int rows, const cx<T> *src, cx<T> *dst,
+                                        const cx<T> *__restrict__ tw, bool scale, bool pair_ok) {
+  using C = FxCfg<T, OP, E, COL>;
+  constexpr int L = C::L, R = fx::radix_of(E, P), LR = L / R;
+  constexpr int TB = C::TB, NT = C::NT;
+  constexpr int NBF = TB * LR;
+  constexpr int ITER = (NBF + NT - 1) / NT;
+  if constexpr (!INPL) {
+#pragma unroll
+    for (int it = 0; it < ITER; ++it) {
+      const int bf = int(threadIdx.x) + it * NT;
+      if (NBF % NT != 0 && bf >= NBF) break;
+      int r, j;
+      fx_rj<TB, LR, COL>(bf, r, j);
+      if (r >= rows) continue;
+      cx<T> v[R];
+      fx_compute<T, OP, E, P, COL, BWD, SRC>(a, row0, r, j, src, tw, pair_ok, v);
+      fx_emit<T, OP, E, P, COL, BWD, DST>(a, row0, r, j, dst, scale, pair_ok, v);
+    }
+  } else {
+    static_assert(SRC == FX_SMEM && DST == FX_SMEM, "in-place passes stay on chip");
+    cx<T> v[ITER][R];
+#pragma unroll
+    for (int it = 0; it < ITER; ++it) {
+      const int bf = int(threadIdx.x) + it * NT;
+      int r, j;
+      fx_rj<TB, LR, COL>(bf, r, j);
+      if ((NBF % NT == 0 || bf < NBF) && r < rows) fx_compute<T, OP, E, P, COL, BWD, SRC>(a, row0, r, j, src, tw, pair_ok, v[it]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITER; ++it) {
+      const int bf = int(threadIdx.x) + it * NT;
+      int r, j;
+      fx_rj<TB, LR, COL>(bf, r, j);
+      if ((NBF % NT == 0 || bf < NBF) && r < rows) fx_emit<T, OP, E, P, COL, BWD, DST>(a, row0, r, j, dst, scale, pair_ok, v[it]);
+    }
+  }
+}
+
+// Passes 1 .. NP-2 in place in buffer A (the first reads global memory or A, the last writes
+// global memory or stays in A).
+template <typename T, int OP, int E, bool COL, bool BWD, int P, int PEND>
+__device__ __forceinline__ void fx_middle(const KArgs &a, uint32_t row0, int rows, cx<T> *buf, const cx<T> *tw,
+                                          bool scale, bool pair_ok) {
+  if constexpr (P < PEND) {
+    fx_pass<T, OP, E, P, COL, BWD, FX_SMEM, FX_SMEM, true>(a, row0, rows, buf, buf, tw, scale, pair_ok);
+    __syncthreads();
+    fx_middle<T, OP, E, COL, BWD, P + 1, PEND>(a, row0, rows, buf, tw, scale, pair_ok);
+  }
+}
+
+template <typename T, int OP, int E, bool COL, bool BWD>
+__global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
+    fixed_kernel(const __grid_constant__ KArgs a, int pair_ok_i) {
+  using C = FxCfg<T, OP, E, COL>;
+  constexpr int L = C::L, NP = C::NP, TB = C::TB, NT = C::NT, PS = C::PS, PITCH = C::PITCH;
+  constexpr int TPR = NT / TB;  // threads per row in the staged loops
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cx<T> *buf = reinterpret_cast<cx<T> *>(smraw);
+  const uint32_t row0 = uint32_t(blockIdx.x) * TB;
+  const int rows = int(min(int64_t(TB), a.nrows - int64_t(row0)));
+  const cx<T> *tw = reinterpret_cast<const cx<T> *>(a.core.tw);
+  const bool scale = a.fct != 1.0;
+  const bool pair_ok = pair_ok_i != 0;
+  const int tid = threadIdx.x;
+  // staged loops: thread -> (row, first element), TPR threads per row
+  const int sr = COL ? (tid & (TB - 1)) : tid / TPR;
+  const int si0 = COL ? tid / TB : tid % TPR;
+
+  if constexpr (OP == OP_C2C) {
+    if constexpr (NP == 1) {
+      fx_pass<T, OP, E, 0, COL, BWD, FX_GLOBAL, FX_GLOBAL>(a, row0, rows, nullptr, nullptr, tw, scale, pair_ok);
+    } else {
+      fx_pass<T, OP, E, 0, COL, BWD, FX_GLOBAL, FX_SMEM>(a, row0, rows, nullptr, buf, tw, scale, pair_ok);
+      __syncthreads();
+      fx_middle<T, OP, E, COL, BWD, 1, NP - 1>(a, row0, rows, buf, tw, scale, pair_ok);
+      fx_pass<T, OP, E, NP - 1, COL, BWD, FX_SMEM, FX_GLOBAL>(a, row0, rows, buf, nullptr, tw, scale, pair_ok);
+    }
+  } else if constexpr (OP == OP_R2C_EVEN) {
+    fx_pass<T, OP, E, 0, COL, false, FX_GLOBAL, FX_SMEM>(a, row0, rows, nullptr, buf, tw, scale, pair_ok);
+    __syncthreads();
+    fx_middle<T, OP, E, COL, false, 1, NP>(a, row0, rows, buf, tw, scale, pair_ok);
+    // split Z_0..Z_{L-1} into X_0..X_L in place
+    const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
+    constexpr int HALF = L / 2 + 1;
+    for (int e = tid; e < rows * HALF; e += NT) {
+      const int r = e / HALF;
+      const int k = e - r * HALF;
+      cx<T> *row = buf + r * PITCH;
+      if (k == 0) {
+        const cx<T> z0 = row[0];
+        row[0] = mk<T>(z0.x + z0.y, T(0));
+        row[L + (L >> PS)] = mk<T>(z0.x - z0.y, T(0));
+      } else {
+        const int kc = L - k;
+        const cx<T> zk = row[k + (k >> PS)], zc = cj<T>(row[kc + (kc >> PS)]);
+        const cx<T> Ev = scl<T>(add<T>(zk, zc), T(0.5));
+        const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
+        const cx<T> u = mul<T>(__ldg(w + k), O);
+        row[k + (k >> PS)] = add<T>(Ev, u);
+        if (kc != k) row[kc + (kc >> PS)] = cj<T>(sub<T>(Ev, u));
+      }
+    }
+    __syncthreads();
+    // staged store of L + 1 bins per row; bins 0 and L carry no interior-bin scale
+    constexpr int UNITS = L + 1;
+    const int64_t s = a.st.axis_stride;
+    const T fct = T(a.fct), bsc = T(a.bscale);
+    const bool cout = a.conj_out != 0;
+    const bool plain = !scale && a.bscale == 1.0 && !cout;
+    if (sr < rows) {
+      cx<T> *p = reinterpret_cast<cx<T> *>(a.out) + side_offset32(a.st, row0 + uint32_t(sr));
+      const cx<T> *row = buf + sr * PITCH;
+      if (plain) {
+#pragma unroll 4
+        for (int i = si0; i < UNITS; i += TPR) p[i * s] = row[i + (i >> PS)];
+      } else {
+        for (int i = si0; i < UNITS; i += TPR) {
+          cx<T> x = row[i + (i >> PS)];
+          if (i != 0 && i != L) x = scl<T>(x, bsc);
+          p[i * s] = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
+        }
+      }
+    }
+  } else {  // OP_C2R_EVEN
+    // staged Hermitian load: every load of the thread is issued before the first shared store
+    constexpr int UNITS = L + 1;
+    constexpr int NLD = (UNITS + TPR - 1) / TPR;
+    {
+      const int64_t s = a.ld.axis_stride;
+      const bool cin = a.conj_in != 0;
+      const T bsc = T(a.bscale);
+      if (sr < rows) {
+        const cx<T> *p = reinterpret_cast<const cx<T> *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
+        cx<T> x[NLD];
+#pragma unroll
+        for (int q = 0; q < NLD; ++q) {
+          const int i = si0 + q * TPR;
+          if (UNITS % TPR == 0 || i < UNITS) x[q] = __ldg(p + i * s);
+        }
+        cx<T> *row = buf + sr * PITCH;
+#pragma unroll
+        for (int q = 0; q < NLD; ++q) {
+          const int i = si0 + q * TPR;
+          if (UNITS % TPR == 0 || i < UNITS) {
+            cx<T> y = x[q];
+            if (cin) y.y = -y.y;
+            if (i == 0 || i == L) y.y = T(0);
+            else y = scl<T>(y, bsc);
+            row[i + (i >> PS)] = y;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // merge X_0..X_L into conj(Z_0..Z_{L-1}) in place
+    const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
+    constexpr int HALF = L / 2 + 1;
+    for (int e = tid; e < rows * HALF; e += NT) {
+      const int r = e / HALF;
+      const int k = e - r * HALF;
+      cx<T> *row = buf + r * PITCH;
+      if (k == 0) {
+        const cx<T> x0 = row[0], xl = row[L + (L >> PS)];
+        const cx<T> A = add<T>(x0, cj<T>(xl)), B = sub<T>(x0, cj<T>(xl));
+        row[0] = cj<T>(add<T>(A, mposi<T>(B)));
+      } else {
+        const int kc = L - k;
+        const cx<T> xk = row[k + (k >> PS)], xc = row[kc + (kc >> PS)];
+        const cx<T> A = add<T>(xk, cj<T>(xc)), B = sub<T>(xk, cj<T>(xc));
+        const cx<T> u = mposi<T>(mulc<T>(B, __ldg(w + k)));
+        row[k + (k >> PS)] = cj<T>(add<T>(A, u));
+        if (kc != k) row[kc + (kc >> PS)] = sub<T>(A, u);
+      }
+    }
+    __syncthreads();
+    fx_middle<T, OP, E, COL, false, 0, NP - 1>(a, row0, rows, buf, tw, scale, pair_ok);
+    fx_pass<T, OP, E, NP - 1, COL, false, FX_SMEM, FX_GLOBAL>(a, row0, rows, buf, nullptr, tw, scale, pair_ok);
+  }
+}
+
+}  // namespace rg

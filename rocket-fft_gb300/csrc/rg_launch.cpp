@@ -13,6 +13,8 @@
 namespace rg {
 
 void launch_axis_f32(int op, const KArgs &a, const LaunchCfg &cfg, cudaStream_t st);
+bool launch_fixed_f32(int op, const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st);
+bool launch_fixed_f64(int op, const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st);
 void launch_axis_f64(int op, const KArgs &a, const LaunchCfg &cfg, cudaStream_t st);
 void launch_pw_f32(int op, const PwArgs &a, cudaStream_t st);
 void launch_pw_f64(int op, const PwArgs &a, cudaStream_t st);
@@ -124,6 +126,15 @@ void launch_axis(DType dt, int op, const KArgs &a, const LaunchCfg &cfg, cudaStr
   if (cfg.grid == 0) return;
   const std::string name = std::string(axis_name(op)) + (dt == DType::F32 ? "_f32" : "_f64");
   timed(name, axis_bytes(dt, op, a), st, [&] {
+    if (cfg.fixed) {
+      const bool done = dt == DType::F32 ? launch_fixed_f32(op, a, cfg.col, cfg.bwd, cfg.pair_ok, st)
+                                         : launch_fixed_f64(op, a, cfg.col, cfg.bwd, cfg.pair_ok, st);
+      if (done) {
+        note_launch();
+        RG_CUDA(cudaGetLastError());
+        return;
+      }
+    }
     if (dt == DType::F32)
       launch_axis_f32(op, a, cfg, st);
     else
@@ -149,6 +160,30 @@ void launch_mirror(DType dt, const MirrorArgs &a, cudaStream_t st) {
           else
             launch_mirror_f64(a, st);
         });
+}
+
+void set_smem_attr(const void *fn, size_t smem) {
+  if (smem <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::vector<std::pair<const void *, int>> done;
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  for (auto &p : done)
+    if (p.first == fn && p.second == dev) return;
+  RG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem_optin())));
+  done.emplace_back(fn, dev);
+}
+
+int sm_count() {
+  static int cache[64] = {};
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && cache[dev]) return cache[dev];
+  int v = 0;
+  RG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+  if (dev < 64) cache[dev] = v;
+  return v;
 }
 
 size_t max_smem_optin() {

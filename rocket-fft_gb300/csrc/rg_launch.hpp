@@ -15,6 +15,13 @@ struct LaunchCfg {
   int threads;
   size_t smem;
   bool pow2 = false;  // use the power-of-two specialised kernel (rg_pow2_kernel.cuh)
+  int stages = 0;     // > 0: persistent pipelined kernel (rg_stream_kernel.cuh) with this many
+                      // stage buffers; `grid` is then the tile count (the launch caps it at
+                      // the CTAs that fit on the device at once)
+  int pair_ok = 0;    // R2C_EVEN input / C2R_EVEN output: real pairs are contiguous and aligned
+  bool fixed = false; // prefer the compile-time-L kernel (rg_fixed_kernel.cuh) when one exists
+  bool col = false;   // fixed kernel: both sides walk across rows
+  bool bwd = false;   // fixed kernel, C2C: conjugate on load and store
 };
 
 // Launch axis_kernel<T, op> with the given configuration.
@@ -68,6 +75,10 @@ void launch_mirror(DType dt, const MirrorArgs &a, cudaStream_t st);
 
 // Largest dynamic shared memory a CTA may use on the current device.
 size_t max_smem_optin();
+// Allow a kernel the large shared-memory carve-out (once per kernel and device).
+void set_smem_attr(const void *fn, size_t smem);
+// Streaming multiprocessors of the current device.
+int sm_count();
 
 uint64_t launch_count();
 void note_launch();

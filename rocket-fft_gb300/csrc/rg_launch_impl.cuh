@@ -1,27 +1,32 @@
 // Typed launch helpers, included once per precision by rg_launch_f32.cu / rg_launch_f64.cu.
 #pragma once
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 
 #include "rg_axis_kernel.cuh"
 #include "rg_pow2_kernel.cuh"
+#include "rg_stream_kernel.cuh"
 #include "rg_error.hpp"
 #include "rg_launch.hpp"
 
 namespace rg {
 
-// Allow the large shared-memory carve-out once per kernel and device.
-inline void ensure_smem_attr(const void *fn, size_t smem) {
-  if (smem <= 48 * 1024) return;
-  static std::mutex mu;
-  static std::vector<std::pair<const void *, int>> done;
-  int dev = 0;
-  RG_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(mu);
-  for (auto &p : done)
-    if (p.first == fn && p.second == dev) return;
-  RG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem_optin())));
-  done.emplace_back(fn, dev);
+inline void ensure_smem_attr(const void *fn, size_t smem) { set_smem_attr(fn, smem); }
+
+// Persistent pipelined kernel: grid = min(tiles, CTAs resident at once).
+template <typename T, int OP, int S>
+void launch_stream_s(const KArgs &a, const LaunchCfg &cfg, const FastDiv &dIn, const FastDiv &dOut,
+                     cudaStream_t st) {
+  const void *fn = reinterpret_cast<const void *>(&stream_kernel<T, OP, S>);
+  ensure_smem_attr(fn, cfg.smem);
+  int per_sm = 0;
+  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, cfg.threads, cfg.smem));
+  RG_CHECK(per_sm > 0, RG_ERR_INTERNAL, "stream kernel does not fit on an SM");
+  const int64_t cap = int64_t(per_sm) * sm_count();
+  const unsigned grid = unsigned(std::min<int64_t>(cfg.grid, cap));
+  StreamParams sp{cfg.pair_ok};
+  stream_kernel<T, OP, S><<<grid, cfg.threads, cfg.smem, st>>>(a, dIn, dOut, sp);
 }
 
 template <typename T, int OP>
@@ -29,6 +34,18 @@ void launch_axis_t(const KArgs &a, const LaunchCfg &cfg, cudaStream_t st) {
   const FastDiv dTB = make_fastdiv(uint32_t(a.TB));
   const FastDiv dIn = make_fastdiv(uint32_t(a.nin > 0 ? a.nin : 1));
   const FastDiv dOut = make_fastdiv(uint32_t(a.nout > 0 ? a.nout : 1));
+  if constexpr (OP == OP_C2C || OP == OP_R2C_EVEN || OP == OP_C2R_EVEN) {
+    if (cfg.stages > 0) {
+      switch (cfg.stages) {
+        case 2: launch_stream_s<T, OP, 2>(a, cfg, dIn, dOut, st); break;
+        case 3: launch_stream_s<T, OP, 3>(a, cfg, dIn, dOut, st); break;
+        default: launch_stream_s<T, OP, 4>(a, cfg, dIn, dOut, st); break;
+      }
+      note_launch();
+      RG_CUDA(cudaGetLastError());
+      return;
+    }
+  }
   if constexpr (OP == OP_C2C || OP == OP_C2C_TW || OP == OP_R2C_EVEN || OP == OP_C2R_EVEN) {
     if (cfg.pow2) {
       const void *fn = reinterpret_cast<const void *>(&pow2_kernel<T, OP>);

@@ -1,5 +1,6 @@
-"""Host-compiled checks of device arithmetic (no GPU needed): the radix butterflies of the
-on-chip FFT against a naive long-double DFT."""
+"""Host-compiled checks of device code (no GPU needed): the radix butterflies of the on-chip FFT
+against a naive long-double DFT, and the compile-time pass schedule of the fixed-length
+kernels against the host core plan."""
 
 from __future__ import annotations
 
@@ -26,5 +27,16 @@ def test_butterflies(tmp_path):
     subprocess.run([_nvcc(), "-O2", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
                     f"-I{ROOT / 'include'}", str(HERE / "native" / "butterflies.cu"), "-o", str(exe)],
                    check=True, capture_output=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_fixed_schedule(tmp_path):
+    exe = tmp_path / "fixed_schedule"
+    r = subprocess.run([_nvcc(), "-O1", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
+                        f"-I{ROOT / 'include'}", str(HERE / "native" / "fixed_schedule.cu"),
+                        str(PKG_DIR / "csrc" / "rg_plan.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
