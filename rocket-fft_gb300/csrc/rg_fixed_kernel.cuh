@@ -53,6 +53,17 @@ __host__ __device__ constexpr int pitch_of(int lsm, int ps, int esz) {
   return p;
 }
 __host__ __device__ constexpr int clampi(int x, int lo, int hi) { return x < lo ? lo : x > hi ? hi : x; }
+// Row walk: when a bank line's worth of lanes spans several rows (g = L / 16 lanes per row in
+// the first pass and the staged loops, g < elements per bank line), rows start g slots apart
+// modulo the bank line so that the rows of one wavefront use disjoint banks.
+__host__ __device__ constexpr int pitch_row(int lsm, int ps, int esz, int L) {
+  const int line = 128 / esz;
+  const int g = L / 16 < line ? L / 16 : line;
+  const int want = g >= line ? 1 : g;
+  int p = lsm + ((lsm - 1) >> ps) + 1;
+  while (p % line != want) ++p;
+  return p;
+}
 
 }  // namespace fx
 
@@ -62,7 +73,7 @@ template <typename T, int OP, int E, bool COL> struct FxCfg {
   static constexpr int ESZ = int(2 * sizeof(T));
   static constexpr int PS = sizeof(T) == 4 ? 4 : 3;
   static constexpr int LSM = OP == OP_C2C ? L : L + 1;
-  static constexpr int PITCH = fx::pitch_of(LSM, PS, ESZ);
+  static constexpr int PITCH = COL ? fx::pitch_of(LSM, PS, ESZ) : fx::pitch_row(LSM, PS, ESZ, L);
   static constexpr int TB = COL ? (sizeof(T) == 4 ? (L <= 256 ? 16 : 8) : (L <= 256 ? 8 : 4))
                                 : ((sizeof(T) == 4 ? 4096 : 2048) / L > 1 ? (sizeof(T) == 4 ? 4096 : 2048) / L : 1);
   static constexpr int NT = fx::clampi(TB * L / 16, 64, 512);
