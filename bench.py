@@ -547,6 +547,43 @@ def run_ours(args):
     peak, peak_kind = peaks()
     traffic = NCU_TRAFFIC.get(dom["name"])
 
+    # tensor-core split-FP16 form: the same steps with the strided c2c passes on tcgen05
+    tc_form = None
+    if rank == 0:
+        prev = rg.set_tc_split(True)
+        try:
+            for i in range(3):
+                step(i)
+            torch.cuda.synchronize()
+            t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0e.record(stream)
+            for i in range(args.steps):
+                step(i)
+            t1e.record(stream)
+            torch.cuda.synchronize()
+            tc_ms = t0e.elapsed_time(t1e)
+            step(0)
+            torch.cuda.synchronize()
+            tc_err = oracle.rel_l2(Xs[0].cpu().numpy(), want)
+            tc_rt = oracle.rel_l2(ys[0].cpu().numpy(), x0)
+            rg.profile_reset()
+            rg.profile_enable(True)
+            for i in range(args.steps):
+                step(i)
+            tc_stats = rg.profile_read()
+            rg.profile_enable(False)
+            tc_form = {"value": 2 * args.steps / (tc_ms / 1e3), "ms_per_step": tc_ms / args.steps,
+                       "vs_plain": (2 * args.steps / (tc_ms / 1e3)) / value,
+                       "r2c_rel_l2_vs_fp64": tc_err, "round_trip_rel_l2": tc_rt,
+                       "tensor_core_errors": rg.tc_error(),
+                       "what": "radix-16 stages of the strided c2c passes as tcgen05 FP16 hi/lo products, "
+                               "FP32 accumulation in tensor memory; r2c/c2r axis plain FP32",
+                       "kernels": [{"name": k["name"], "launches": k["launches"], "ms": k["total_ms"],
+                                    "gbs": k["bytes"] / (k["total_ms"] / 1e3) / 1e9 if k["total_ms"] else None}
+                                   for k in tc_stats]}
+        finally:
+            rg.set_tc_split(prev)
+
     # e2e: the same round trip through the C ABI on pinned host arrays
     e2e = None
     if rank == 0:
@@ -597,6 +634,9 @@ def run_ours(args):
                          "share": s["total_ms"] / total_ms,
                          "gbs": s["bytes"] / (s["total_ms"] / 1e3) / 1e9 if s["total_ms"] else None} for s in stats],
             "accuracy": acc,
+            "forms": {"plain_fp32": {"value": value, "ms_per_step": ms / args.steps,
+                                     "r2c_rel_l2_vs_fp64": acc.get("r2c_rel_l2_vs_fp64")},
+                      "tc_split_fp16": tc_form},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,

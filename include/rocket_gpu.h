@@ -214,6 +214,20 @@ int rocketgpu_c2c_noalloc(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocke
                           rocketgpu_arystruct_t *axes, bool forward, double fct, uint64_t nthreads,
                           void *stream, char *errbuf, size_t errlen);
 
+/* Tensor-core split-FP16 form (no counterpart in the reference; a precision form of the same
+ * transforms). While enabled (process-wide), complex64 transforms of length 256 along strided
+ * axes run their two radix-16 stages as tcgen05 matrix products on FP16 hi/lo operand splits
+ * with FP32 accumulation (about 22 significant bits per product); every other job keeps the
+ * plain FP32 kernels. rocketgpu_set_tc_split returns the previous setting.
+ * rocketgpu_tc_error returns 1 if a tensor-core kernel gave up waiting for its matrix products
+ * since the library was loaded (0 otherwise, negative status on failure).
+ * rocketgpu_tc_selftest computes D = A B^T + A B2^T + A2 B^T + A2 B2^T on the tensor cores through the
+ * same operand layout, descriptors and tensor-memory path as the transform kernels: A, A2
+ * 256 x 32, B, B2 32 x 32 float16 (row-major, device), D 256 x 32 float32 (device). */
+int rocketgpu_set_tc_split(int on);
+int rocketgpu_tc_error(void *stream);
+int rocketgpu_tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D, void *stream);
+
 /* Library version string. */
 const char *rocketgpu_version(void);
 

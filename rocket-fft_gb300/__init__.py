@@ -30,6 +30,9 @@ from .pocketfft import (  # noqa: F401
     r2r_genuine_hartley,
     r2r_separable_hartley,
     set_stream,
+    set_tc_split,
+    tc_error,
+    tc_selftest,
     version,
 )
 

@@ -88,6 +88,12 @@ def _declare(lib):
     lib.rocketgpu_profile_read.argtypes = [ctypes.POINTER(KStat), ctypes.c_int]
     lib.rocketgpu_profile_read.restype = i32
     lib.rocketgpu_profile_reset.restype = None
+    lib.rocketgpu_set_tc_split.argtypes = [i32]
+    lib.rocketgpu_set_tc_split.restype = i32
+    lib.rocketgpu_tc_error.argtypes = [P]
+    lib.rocketgpu_tc_error.restype = i32
+    lib.rocketgpu_tc_selftest.argtypes = [P, P, P, P, P, P]
+    lib.rocketgpu_tc_selftest.restype = i32
     return lib
 
 

@@ -492,6 +492,22 @@ RG_EXPORT int rocketgpu_plan_cache_clear(void) {
 
 RG_EXPORT uint64_t rocketgpu_launch_count(void) { return rg::launch_count(); }
 
+RG_EXPORT int rocketgpu_set_tc_split(int on) { return rg::set_tc_split(on != 0); }
+
+RG_EXPORT int rocketgpu_tc_error(void *stream) {
+  int flag = 0;
+  const int st = guarded([&] { flag = rg::tc_error_flag(static_cast<cudaStream_t>(stream)); });
+  return st == RG_OK ? flag : -st;
+}
+
+RG_EXPORT int rocketgpu_tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D,
+                                    void *stream) {
+  return guarded([&] {
+    RG_CHECK(A && A2 && B && B2 && D, RG_ERR_ARG, "null operand");
+    rg::tc_selftest(A, A2, B, B2, D, static_cast<cudaStream_t>(stream));
+  });
+}
+
 RG_EXPORT void rocketgpu_profile_enable(int on) { rg::profile_enable(on != 0); }
 
 RG_EXPORT int rocketgpu_profile_read(rocketgpu_kstat_t *out, int max) {

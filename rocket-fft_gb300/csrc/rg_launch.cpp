@@ -22,6 +22,10 @@ void launch_mirror_f32(const MirrorArgs &a, cudaStream_t st);
 void launch_mirror_f64(const MirrorArgs &a, cudaStream_t st);
 
 static std::atomic<uint64_t> g_launches{0};
+static std::atomic<int> g_tc{0};
+
+bool tc_split_enabled() { return g_tc.load(std::memory_order_relaxed) != 0; }
+int set_tc_split(bool on) { return g_tc.exchange(on ? 1 : 0); }
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
@@ -124,6 +128,14 @@ void profile_reset() {
 
 void launch_axis(DType dt, int op, const KArgs &a, const LaunchCfg &cfg, cudaStream_t st) {
   if (cfg.grid == 0) return;
+  if (cfg.fixed && dt == DType::F32 && op == OP_C2C && cfg.col && a.core.L == 256 && tc_split_enabled()) {
+    timed("axis_c2c_tc_f32", axis_bytes(dt, op, a), st, [&] {
+      RG_CHECK(launch_tc_c2c(a, cfg.col, cfg.bwd, st), RG_ERR_INTERNAL, "tensor-core kernel rejected its job");
+      note_launch();
+      RG_CUDA(cudaGetLastError());
+    });
+    return;
+  }
   const std::string name = std::string(axis_name(op)) + (dt == DType::F32 ? "_f32" : "_f64");
   timed(name, axis_bytes(dt, op, a), st, [&] {
     if (cfg.fixed) {

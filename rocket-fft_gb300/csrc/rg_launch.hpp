@@ -80,6 +80,13 @@ void set_smem_attr(const void *fn, size_t smem);
 // Streaming multiprocessors of the current device.
 int sm_count();
 
+// Tensor-core split-FP16 form (rg_tc_kernel.cu).
+bool tc_split_enabled();
+int set_tc_split(bool on);
+bool launch_tc_c2c(const KArgs &a, bool col, bool bwd, cudaStream_t st);
+int tc_error_flag(cudaStream_t st);
+void tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D, cudaStream_t st);
+
 uint64_t launch_count();
 void note_launch();
 

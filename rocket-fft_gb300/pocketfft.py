@@ -348,6 +348,44 @@ def set_stream(stream):
     _lib.load().rocketgpu_set_stream(ctypes.c_void_p(stream) if stream else None)
 
 
+def set_tc_split(on=True):
+    """Switch the tensor-core split-FP16 form on or off (process-wide); returns the previous
+    setting. While on, complex64 length-256 transforms along strided axes run their radix-16
+    stages on the tensor cores (FP16 hi/lo operands, FP32 accumulation); everything else
+    keeps the plain kernels. No counterpart in rocket-fft."""
+    return bool(_lib.load().rocketgpu_set_tc_split(1 if on else 0))
+
+
+def tc_error(stream=None):
+    """1 if a tensor-core kernel gave up waiting for its matrix products since load, else 0."""
+    r = int(_lib.load().rocketgpu_tc_error(ctypes.c_void_p(_stream_int(stream)) if stream else None))
+    if r < 0:
+        _raise_status(-r, "rocketgpu_tc_error")
+    return r
+
+
+def tc_selftest(A, A2, B, B2, D):
+    """D = A B^T + A B2^T + A2 B^T + A2 B2^T on the tensor cores (device torch tensors: A, A2 float16
+    256 x 32, B, B2 float16 32 x 32, D float32 256 x 32, all contiguous), through the operand
+    layout and tensor-memory path of the transform kernels. Runs on the current torch stream."""
+    import torch
+
+    for t, shape, dt in ((A, (256, 32), torch.float16), (A2, (256, 32), torch.float16),
+                         (B, (32, 32), torch.float16), (B2, (32, 32), torch.float16),
+                         (D, (256, 32), torch.float32)):
+        if tuple(t.shape) != shape or t.dtype != dt or not t.is_cuda or not t.is_contiguous():
+            raise TypingError("tc_selftest: operand shape, dtype or layout")
+    st = torch.cuda.current_stream(A.device).cuda_stream
+    r = _lib.load().rocketgpu_tc_selftest(A.data_ptr(), A2.data_ptr(), B.data_ptr(), B2.data_ptr(),
+                                          D.data_ptr(), ctypes.c_void_p(st) if st else None)
+    if r != 0:
+        _raise_status(r, "rocketgpu_tc_selftest")
+
+
+def _stream_int(stream):
+    return stream if isinstance(stream, int) else stream.cuda_stream
+
+
 def plan_cache_entries():
     return int(_lib.load().rocketgpu_plan_cache_entries())
 
