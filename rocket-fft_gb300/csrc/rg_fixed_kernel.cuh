@@ -266,6 +266,94 @@ __device__ __forceinline__ void fx_pass(const KArgs &a, uint32_t row0, int rows,
   }
 }
 
+// Last pass of R2C_EVEN with the split fused in (last radix <= 8). Unit (r, u) transforms the
+// butterflies j1 = u and j2 = NS - u (u = 0: j1 = 0, j2 = NS / 2) of row r, whose outputs
+// Z_{j + q NS} hold both members of every pair (k, L - k); it splits them in registers,
+//     X_k = E + W_2L^k O,  X_{L-k} = conj(E - W_2L^k O),  E = (Z_k + conj Z_{L-k}) / 2,
+//     O = -i (Z_k - conj Z_{L-k}) / 2,   X_0 = Re Z_0 + Im Z_0,  X_L = Re Z_0 - Im Z_0,
+// and stores X straight to global memory.
+template <typename T, int E, bool COL>
+__device__ __forceinline__ void fx_r2c_last_split(const KArgs &a, uint32_t row0, int rows, const cx<T> *buf,
+                                                  const cx<T> *__restrict__ tw) {
+  using C = FxCfg<T, OP_R2C_EVEN, E, COL>;
+  constexpr int L = C::L, P = C::NP - 1, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P);
+  constexpr int TWO = fx::tw_of(E, P);
+  static_assert(NS == LR && R <= 8 && R >= 2, "last pass");
+  constexpr int TB = C::TB, NT = C::NT, PS = C::PS, PITCH = C::PITCH;
+  constexpr int UPR = LR / 2;  // units per row
+  constexpr int NU = TB * UPR;
+  constexpr int ITER = (NU + NT - 1) / NT;
+  const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
+  const int64_t s = a.st.axis_stride;
+  const T fct = T(a.fct), bsc = T(a.bscale);
+  const bool cout = a.conj_out != 0;
+  const bool plain = a.fct == 1.0 && a.bscale == 1.0 && !cout;
+#pragma unroll
+  for (int it = 0; it < ITER; ++it) {
+    const int unit = int(threadIdx.x) + it * NT;
+    if (NU % NT != 0 && unit >= NU) break;
+    int r, u;
+    if constexpr (COL) {
+      r = unit & (TB - 1);
+      u = unit / TB;
+    } else {
+      r = unit / UPR;
+      u = unit % UPR;
+    }
+    if (r >= rows) continue;
+    const int j1 = u, j2 = u == 0 ? NS / 2 : NS - u;
+    cx<T> v1[R], v2[R];
+    {
+      const cx<T> *sp = buf + r * PITCH;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        v1[k] = sp[fx_pos<PS, LR>(j1, k)];
+        v2[k] = sp[fx_pos<PS, LR>(j2, k)];
+      }
+      const cx<T> *t1 = tw + TWO + j1, *t2 = tw + TWO + j2;
+#pragma unroll
+      for (int k = 1; k < R; ++k) {
+        v1[k] = mul<T>(v1[k], __ldg(t1 + (k - 1) * NS));
+        v2[k] = mul<T>(v2[k], __ldg(t2 + (k - 1) * NS));
+      }
+      dft<T, R>(v1);
+      dft<T, R>(v2);
+    }
+    cx<T> *p = reinterpret_cast<cx<T> *>(a.out) + side_offset32(a.st, row0 + uint32_t(r));
+    auto put = [&](int i, cx<T> x) {
+      if (!plain) {
+        if (i != 0 && i != L) x = scl<T>(x, bsc);
+        x = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
+      }
+      p[i * s] = x;
+    };
+    // pair (ka, L - ka), ka <= L / 2, from za = Z_ka and zb = Z_{L-ka}
+    auto split = [&](int ka, cx<T> za, cx<T> zb, bool self) {
+      const cx<T> zc = cj<T>(zb);
+      const cx<T> Ev = scl<T>(add<T>(za, zc), T(0.5));
+      const cx<T> O = mnegi<T>(scl<T>(sub<T>(za, zc), T(0.5)));
+      const cx<T> t = mul<T>(__ldg(w + ka), O);
+      put(ka, add<T>(Ev, t));
+      if (!self) put(L - ka, cj<T>(sub<T>(Ev, t)));
+    };
+    if (u == 0) {
+      put(0, mk<T>(v1[0].x + v1[0].y, T(0)));
+      put(L, mk<T>(v1[0].x - v1[0].y, T(0)));
+#pragma unroll
+      for (int q = 1; q < R / 2; ++q) split(q * NS, v1[q], v1[R - q], false);
+      split(L / 2, v1[R / 2], v1[R / 2], true);
+#pragma unroll
+      for (int q = 0; q < R / 2; ++q) split(NS / 2 + q * NS, v2[q], v2[R - 1 - q], false);
+    } else {
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        if (q < R / 2) split(u + q * NS, v1[q], v2[R - 1 - q], false);
+        else split(j2 + (R - 1 - q) * NS, v2[R - 1 - q], v1[q], false);
+      }
+    }
+  }
+}
+
 // Passes 1 .. NP-2 in place in buffer A (the first reads global memory or A, the last writes
 // global memory or stays in A).
 template <typename T, int OP, int E, bool COL, bool BWD, int P, int PEND>
@@ -308,98 +396,100 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
   } else if constexpr (OP == OP_R2C_EVEN) {
     fx_pass<T, OP, E, 0, COL, false, FX_GLOBAL, FX_SMEM>(a, row0, rows, nullptr, buf, tw, scale, pair_ok);
     __syncthreads();
-    fx_middle<T, OP, E, COL, false, 1, NP>(a, row0, rows, buf, tw, scale, pair_ok);
-    // split Z_0..Z_{L-1} into X_0..X_L in place
-    const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
-    constexpr int HALF = L / 2 + 1;
-    for (int e = tid; e < rows * HALF; e += NT) {
-      const int r = e / HALF;
-      const int k = e - r * HALF;
-      cx<T> *row = buf + r * PITCH;
-      if (k == 0) {
-        const cx<T> z0 = row[0];
-        row[0] = mk<T>(z0.x + z0.y, T(0));
-        row[L + (L >> PS)] = mk<T>(z0.x - z0.y, T(0));
-      } else {
-        const int kc = L - k;
-        const cx<T> zk = row[k + (k >> PS)], zc = cj<T>(row[kc + (kc >> PS)]);
-        const cx<T> Ev = scl<T>(add<T>(zk, zc), T(0.5));
-        const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
-        const cx<T> u = mul<T>(__ldg(w + k), O);
-        row[k + (k >> PS)] = add<T>(Ev, u);
-        if (kc != k) row[kc + (kc >> PS)] = cj<T>(sub<T>(Ev, u));
-      }
-    }
-    __syncthreads();
-    // staged store of L + 1 bins per row; bins 0 and L carry no interior-bin scale
-    constexpr int UNITS = L + 1;
-    const int64_t s = a.st.axis_stride;
-    const T fct = T(a.fct), bsc = T(a.bscale);
-    const bool cout = a.conj_out != 0;
-    const bool plain = !scale && a.bscale == 1.0 && !cout;
-    if (sr < rows) {
-      cx<T> *p = reinterpret_cast<cx<T> *>(a.out) + side_offset32(a.st, row0 + uint32_t(sr));
-      const cx<T> *row = buf + sr * PITCH;
-      if (plain) {
-#pragma unroll 4
-        for (int i = si0; i < UNITS; i += TPR) p[i * s] = row[i + (i >> PS)];
-      } else {
-        for (int i = si0; i < UNITS; i += TPR) {
-          cx<T> x = row[i + (i >> PS)];
-          if (i != 0 && i != L) x = scl<T>(x, bsc);
-          p[i * s] = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
+    if constexpr (NP >= 2 && fx::radix_of(E, NP - 1) <= 8) {
+      fx_middle<T, OP, E, COL, false, 1, NP - 1>(a, row0, rows, buf, tw, scale, pair_ok);
+      fx_r2c_last_split<T, E, COL>(a, row0, rows, buf, tw);
+    } else {
+      fx_middle<T, OP, E, COL, false, 1, NP>(a, row0, rows, buf, tw, scale, pair_ok);
+      // split Z_0..Z_{L-1} into X_0..X_L in place
+      const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
+      constexpr int HALF = L / 2 + 1;
+      for (int e = tid; e < rows * HALF; e += NT) {
+        const int r = e / HALF;
+        const int k = e - r * HALF;
+        cx<T> *row = buf + r * PITCH;
+        if (k == 0) {
+          const cx<T> z0 = row[0];
+          row[0] = mk<T>(z0.x + z0.y, T(0));
+          row[L + (L >> PS)] = mk<T>(z0.x - z0.y, T(0));
+        } else {
+          const int kc = L - k;
+          const cx<T> zk = row[k + (k >> PS)], zc = cj<T>(row[kc + (kc >> PS)]);
+          const cx<T> Ev = scl<T>(add<T>(zk, zc), T(0.5));
+          const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
+          const cx<T> u = mul<T>(__ldg(w + k), O);
+          row[k + (k >> PS)] = add<T>(Ev, u);
+          if (kc != k) row[kc + (kc >> PS)] = cj<T>(sub<T>(Ev, u));
         }
       }
-    }
-  } else {  // OP_C2R_EVEN
-    // staged Hermitian load: every load of the thread is issued before the first shared store
-    constexpr int UNITS = L + 1;
-    constexpr int NLD = (UNITS + TPR - 1) / TPR;
-    {
-      const int64_t s = a.ld.axis_stride;
-      const bool cin = a.conj_in != 0;
-      const T bsc = T(a.bscale);
+      __syncthreads();
+      // staged store of L + 1 bins per row; bins 0 and L carry no interior-bin scale
+      constexpr int UNITS = L + 1;
+      const int64_t s = a.st.axis_stride;
+      const T fct = T(a.fct), bsc = T(a.bscale);
+      const bool cout = a.conj_out != 0;
+      const bool plain = !scale && a.bscale == 1.0 && !cout;
       if (sr < rows) {
-        const cx<T> *p = reinterpret_cast<const cx<T> *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
-        cx<T> x[NLD];
-#pragma unroll
-        for (int q = 0; q < NLD; ++q) {
-          const int i = si0 + q * TPR;
-          if (UNITS % TPR == 0 || i < UNITS) x[q] = __ldg(p + i * s);
-        }
-        cx<T> *row = buf + sr * PITCH;
-#pragma unroll
-        for (int q = 0; q < NLD; ++q) {
-          const int i = si0 + q * TPR;
-          if (UNITS % TPR == 0 || i < UNITS) {
-            cx<T> y = x[q];
-            if (cin) y.y = -y.y;
-            if (i == 0 || i == L) y.y = T(0);
-            else y = scl<T>(y, bsc);
-            row[i + (i >> PS)] = y;
+        cx<T> *p = reinterpret_cast<cx<T> *>(a.out) + side_offset32(a.st, row0 + uint32_t(sr));
+        const cx<T> *row = buf + sr * PITCH;
+        if (plain) {
+#pragma unroll 4
+          for (int i = si0; i < UNITS; i += TPR) p[i * s] = row[i + (i >> PS)];
+        } else {
+          for (int i = si0; i < UNITS; i += TPR) {
+            cx<T> x = row[i + (i >> PS)];
+            if (i != 0 && i != L) x = scl<T>(x, bsc);
+            p[i * s] = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
           }
         }
       }
     }
-    __syncthreads();
-    // merge X_0..X_L into conj(Z_0..Z_{L-1}) in place
-    const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
-    constexpr int HALF = L / 2 + 1;
-    for (int e = tid; e < rows * HALF; e += NT) {
-      const int r = e / HALF;
-      const int k = e - r * HALF;
-      cx<T> *row = buf + r * PITCH;
-      if (k == 0) {
-        const cx<T> x0 = row[0], xl = row[L + (L >> PS)];
-        const cx<T> A = add<T>(x0, cj<T>(xl)), B = sub<T>(x0, cj<T>(xl));
-        row[0] = cj<T>(add<T>(A, mposi<T>(B)));
-      } else {
-        const int kc = L - k;
-        const cx<T> xk = row[k + (k >> PS)], xc = row[kc + (kc >> PS)];
-        const cx<T> A = add<T>(xk, cj<T>(xc)), B = sub<T>(xk, cj<T>(xc));
-        const cx<T> u = mposi<T>(mulc<T>(B, __ldg(w + k)));
-        row[k + (k >> PS)] = cj<T>(add<T>(A, u));
-        if (kc != k) row[kc + (kc >> PS)] = sub<T>(A, u);
+  } else {  // OP_C2R_EVEN
+    // staged Hermitian load fused with the merge: the thread takes the pairs (i, L - i),
+    // i = first + q * TPR <= L / 2, loads both bins (all loads issued before any use), applies
+    // the input conversion (conjugation, zero imaginary parts of bins 0 and L, interior-bin
+    // scale) and writes conj(Z_i) and conj(Z_{L-i}):
+    //     A = X_i + conj X_{L-i},  B = X_i - conj X_{L-i},  U = i B conj(W_2L^i),
+    //     conj Z_i = conj(A + U),  conj Z_{L-i} = A - U   (i = 0: conj Z_0 = conj(A + i B)).
+    constexpr int HP = L / 2 + 1;
+    constexpr int NQ = (HP + TPR - 1) / TPR;
+    if (sr < rows) {
+      const int64_t s = a.ld.axis_stride;
+      const bool cin = a.conj_in != 0;
+      const T bsc = T(a.bscale);
+      const cx<T> *p = reinterpret_cast<const cx<T> *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
+      const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux);
+      cx<T> xa[NQ], xb[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int i = si0 + q * TPR;
+        if (HP % TPR == 0 || i < HP) {
+          xa[q] = __ldg(p + i * s);
+          xb[q] = __ldg(p + (L - i) * s);
+        }
+      }
+      auto fix = [&](int i, cx<T> x) {
+        if (cin) x.y = -x.y;
+        if (i == 0 || i == L) x.y = T(0);
+        else x = scl<T>(x, bsc);
+        return x;
+      };
+      cx<T> *row = buf + sr * PITCH;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int i = si0 + q * TPR;
+        if (HP % TPR == 0 || i < HP) {
+          const cx<T> x = fix(i, xa[q]), y = fix(L - i, xb[q]);
+          const cx<T> A = add<T>(x, cj<T>(y)), B = sub<T>(x, cj<T>(y));
+          if (i == 0) {
+            row[0] = cj<T>(add<T>(A, mposi<T>(B)));
+          } else {
+            const int kc = L - i;
+            const cx<T> U = mposi<T>(mulc<T>(B, __ldg(w + i)));
+            row[i + (i >> PS)] = cj<T>(add<T>(A, U));
+            if (kc != i) row[kc + (kc >> PS)] = sub<T>(A, U);
+          }
+        }
       }
     }
     __syncthreads();
