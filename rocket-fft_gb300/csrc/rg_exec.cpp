@@ -334,14 +334,17 @@ void run_job(const Job &j, cudaStream_t st) {
   }
   // compile-time-L kernel: power-of-two L, both sides walking alike, 32-bit row numbers,
   // C2C conjugating on both sides or neither
-  if (pow2 && !stream && fixed_enabled() && (j.op == OP_C2C || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN) &&
-      ld.colmap == sd.colmap && j.nrows < (int64_t(1) << 31) && (j.op != OP_C2C || j.cin == j.cout) &&
-      set_fastdivs(a.ld) && set_fastdivs(a.st)) {
+  const bool pow2L = j.L >= 2 && (j.L & (j.L - 1)) == 0 && pow2_enabled();
+  const bool fixed_op = j.op == OP_C2C || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN || j.op == OP_DCT2 ||
+                        j.op == OP_DCT3;
+  if (pow2L && !stream && fixed_enabled() && fixed_op && ld.colmap == sd.colmap &&
+      j.nrows < (int64_t(1) << 31) && (j.op != OP_C2C || j.cin == j.cout) && set_fastdivs(a.ld) &&
+      set_fastdivs(a.st)) {
     cfg.fixed = true;
     cfg.col = ld.colmap != 0;
     cfg.bwd = j.op == OP_C2C && j.cin;
     const size_t rsz = real_size(j.dt);
-    if (j.op == OP_R2C_EVEN) {
+    if (j.op == OP_R2C_EVEN || j.op == OP_DCT2) {
       bool ok = ld.axis_stride == 1 && reinterpret_cast<uintptr_t>(j.in) % (2 * rsz) == 0;
       for (int d = 0; d < ld.nbd; ++d) ok = ok && ld.bstride[d] % 2 == 0;
       cfg.pair_ok = ok ? 1 : 0;

@@ -19,6 +19,8 @@
 //             (im, re)-swapped data, swapped back on store (swap(F(swap(x))) = conj(F(conj(x))))
 //   R2C_EVEN  real pairs -> A -> ... (all passes on chip), split into X_0..X_L, staged store
 //   C2R_EVEN  staged Hermitian load, merge into conj(Z), passes, real pairs to global
+//   DCT2/3    (DCT/DST types II and III by Makhoul's n-point complex FFT) staged load with the
+//             reordering / pre-twiddle, passes, post-twiddle / un-reordering on the last store
 #pragma once
 #include "rg_axis_kernel.cuh"
 
@@ -72,7 +74,7 @@ template <typename T, int OP, int E, bool COL> struct FxCfg {
   static constexpr int NP = fx::np_of(E);
   static constexpr int ESZ = int(2 * sizeof(T));
   static constexpr int PS = sizeof(T) == 4 ? 4 : 3;
-  static constexpr int LSM = OP == OP_C2C ? L : L + 1;
+  static constexpr int LSM = (OP == OP_C2C || OP == OP_DCT2 || OP == OP_DCT3) ? L : L + 1;
   static constexpr int PITCH = COL ? fx::pitch_of(LSM, PS, ESZ) : fx::pitch_row(LSM, PS, ESZ, L);
   static constexpr int TB = COL ? (sizeof(T) == 4 ? (L <= 256 ? 16 : 8) : (L <= 256 ? 8 : 4))
                                 : ((sizeof(T) == 4 ? 4096 : 2048) / L > 1 ? (sizeof(T) == 4 ? 4096 : 2048) / L : 1);
@@ -177,7 +179,36 @@ __device__ __forceinline__ void fx_emit(const KArgs &a, uint32_t row0, int r, in
     const int64_t s = a.st.axis_stride;
     const int64_t off = side_offset32(a.st, row0 + uint32_t(r));
     const T fct = T(a.fct);
-    if constexpr (OP == OP_C2R_EVEN) {
+    if constexpr (OP == OP_DCT2) {
+      // y_pos = 2 Re(e^{-i pi kk / 2n} V_kk) * fct, pos = kk (DCT) or n-1-kk (DST); pos 0 x e0
+      constexpr int L = C::L;
+      T *out = reinterpret_cast<T *>(a.out) + off;
+      const cx<T> *tw2 = reinterpret_cast<const cx<T> *>(a.aux);
+      const bool sine = (a.flags & 2) != 0;
+      const T e0 = T(a.e0);
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int kk = base + k * NS;
+        const cx<T> t = __ldg(tw2 + kk);
+        T y = T(2) * (v[k].x * t.x - v[k].y * t.y) * fct;
+        const int pos = sine ? L - 1 - kk : kk;
+        if (pos == 0) y *= e0;
+        out[pos * s] = y;
+      }
+    } else if constexpr (OP == OP_DCT3) {
+      // y_2j = Re v_j (j < n/2), y_2(n-1-j)+1 = Re v_j (j >= n/2); DST: odd outputs negated
+      constexpr int L = C::L;
+      T *out = reinterpret_cast<T *>(a.out) + off;
+      const bool sine = (a.flags & 2) != 0;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int jj = base + k * NS;
+        const bool odd = jj >= L / 2;
+        const int pos = odd ? 2 * (L - 1 - jj) + 1 : 2 * jj;
+        const T y = v[k].x * fct;
+        out[pos * s] = (sine && odd) ? -y : y;
+      }
+    } else if constexpr (OP == OP_C2R_EVEN) {
       // (x_2i, x_2i+1) = (Re F_i, -Im F_i) * fct
       T *out = reinterpret_cast<T *>(a.out) + off;
       if (pair_ok) {
@@ -327,28 +358,61 @@ __device__ __forceinline__ void fx_r2c_last_split(const KArgs &a, uint32_t row0,
       }
       p[i * s] = x;
     };
-    // pair (ka, L - ka), ka <= L / 2, from za = Z_ka and zb = Z_{L-ka}
-    auto split = [&](int ka, cx<T> za, cx<T> zb, bool self) {
-      const cx<T> zc = cj<T>(zb);
-      const cx<T> Ev = scl<T>(add<T>(za, zc), T(0.5));
-      const cx<T> O = mnegi<T>(scl<T>(sub<T>(za, zc), T(0.5)));
-      const cx<T> t = mul<T>(__ldg(w + ka), O);
-      put(ka, add<T>(Ev, t));
-      if (!self) put(L - ka, cj<T>(sub<T>(Ev, t)));
-    };
-    if (u == 0) {
-      put(0, mk<T>(v1[0].x + v1[0].y, T(0)));
-      put(L, mk<T>(v1[0].x - v1[0].y, T(0)));
+    // Slot q of a unit: the pair (ka, L - ka), ka <= L / 2, from za = Z_ka, zb = Z_{L-ka}:
+    //   u >= 1, q < R/2:   (u + q NS, v1[q], v2[R-1-q]);  q >= R/2: (j2 + (R-1-q) NS, v2[R-1-q], v1[q])
+    //   u = 0:   q = 0: (0, v1[0], v1[0]) -- the split formula then gives X_0 and X_L;
+    //            1 <= q < R/2: (q NS, v1[q], v1[R-q]);  q = R/2: (L/2, v1[R/2], v1[R/2]), one output;
+    //            R/2 < q <= R: (NS/2 + (q-R/2-1) NS, v2[q-R/2-1], v2[R-1-(q-R/2-1)])
+    // All lanes run the same R + 1 slots (the last only for u = 0); operands are selected, not
+    // branched on, so the unit-0 lanes of a warp do not diverge.
+    const bool u0 = u == 0;
 #pragma unroll
-      for (int q = 1; q < R / 2; ++q) split(q * NS, v1[q], v1[R - q], false);
-      split(L / 2, v1[R / 2], v1[R / 2], true);
-#pragma unroll
-      for (int q = 0; q < R / 2; ++q) split(NS / 2 + q * NS, v2[q], v2[R - 1 - q], false);
-    } else {
-#pragma unroll
-      for (int q = 0; q < R; ++q) {
-        if (q < R / 2) split(u + q * NS, v1[q], v2[R - 1 - q], false);
-        else split(j2 + (R - 1 - q) * NS, v2[R - 1 - q], v1[q], false);
+    for (int q = 0; q <= R; ++q) {
+      // general unit
+      int kg = 0;
+      cx<T> zag = v1[0], zbg = v1[0];
+      if (q < R / 2) {
+        kg = u + q * NS;
+        zag = v1[q];
+        zbg = v2[R - 1 - q];
+      } else if (q < R) {
+        kg = j2 + (R - 1 - q) * NS;
+        zag = v2[R - 1 - q];
+        zbg = v1[q];
+      }
+      // unit 0
+      int k0;
+      cx<T> za0, zb0;
+      bool two0 = true;
+      if (q == 0) {
+        k0 = 0;
+        za0 = v1[0];
+        zb0 = v1[0];
+      } else if (q < R / 2) {
+        k0 = q * NS;
+        za0 = v1[q];
+        zb0 = v1[R - q];
+      } else if (q == R / 2) {
+        k0 = L / 2;
+        za0 = v1[R / 2];
+        zb0 = v1[R / 2];
+        two0 = false;
+      } else {
+        const int qq = q - R / 2 - 1;
+        k0 = NS / 2 + qq * NS;
+        za0 = v2[qq];
+        zb0 = v2[R - 1 - qq];
+      }
+      const int ka = u0 ? k0 : kg;
+      const cx<T> za = u0 ? za0 : zag, zb = u0 ? zb0 : zbg;
+      const bool two = u0 ? two0 : true;
+      if (u0 || q < R) {
+        const cx<T> zc = cj<T>(zb);
+        const cx<T> Ev = scl<T>(add<T>(za, zc), T(0.5));
+        const cx<T> O = mnegi<T>(scl<T>(sub<T>(za, zc), T(0.5)));
+        const cx<T> t = mul<T>(__ldg(w + ka), O);
+        put(ka, add<T>(Ev, t));
+        if (two) put(L - ka, cj<T>(sub<T>(Ev, t)));
       }
     }
   }
@@ -444,6 +508,71 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
         }
       }
     }
+  } else if constexpr (OP == OP_DCT2 || OP == OP_DCT3) {
+    const int64_t s = a.ld.axis_stride;
+    const bool sine = (a.flags & 2) != 0;
+    if constexpr (OP == OP_DCT2) {
+      // Makhoul order: v_m = x_2m, v_{n-1-m} = x_2m+1 (DST: odd inputs negated), as complex
+      // numbers with zero imaginary part; the thread loads the pairs m = first + q * TPR
+      constexpr int HP = L / 2, NQ = (HP + TPR - 1) / TPR;
+      if (sr < rows) {
+        const T *p = reinterpret_cast<const T *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
+        cx<T> xv[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int m = si0 + q * TPR;
+          if (HP % TPR == 0 || m < HP) {
+            if (pair_ok) xv[q] = __ldg(reinterpret_cast<const cx<T> *>(p) + m);
+            else xv[q] = mk<T>(__ldg(p + 2 * m * s), __ldg(p + (2 * m + 1) * s));
+          }
+        }
+        cx<T> *row = buf + sr * PITCH;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int m = si0 + q * TPR;
+          if (HP % TPR == 0 || m < HP) {
+            const int mc = L - 1 - m;
+            row[m + (m >> PS)] = mk<T>(xv[q].x, T(0));
+            row[mc + (mc >> PS)] = mk<T>(sine ? -xv[q].y : xv[q].y, T(0));
+          }
+        }
+      }
+    } else {
+      // conj(V_i), V_i = (x''_i - i x''_{n-i}) e^{i pi i / 2n}, x''_q = x_q (DCT) or x_{n-1-q}
+      // (DST), x''_n = 0; input element 0 weighted e0
+      constexpr int NQ = (L + TPR - 1) / TPR;
+      if (sr < rows) {
+        const T *p = reinterpret_cast<const T *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
+        const cx<T> *tw3 = reinterpret_cast<const cx<T> *>(a.aux);
+        const T e0 = T(a.e0);
+        cx<T> xv[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int i = si0 + q * TPR;
+          if (L % TPR == 0 || i < L) {
+            const int sa = sine ? L - 1 - i : i;
+            const T xa = __ldg(p + sa * s);
+            const T xb = i == 0 ? T(0) : __ldg(p + (sine ? i - 1 : L - i) * s);
+            xv[q] = mk<T>(xa, xb);
+          }
+        }
+        cx<T> *row = buf + sr * PITCH;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int i = si0 + q * TPR;
+          if (L % TPR == 0 || i < L) {
+            cx<T> x = xv[q];
+            if (sine ? i == L - 1 : i == 0) x.x *= e0;
+            if (sine && i == 1) x.y *= e0;
+            const cx<T> t = __ldg(tw3 + i);  // e^{-i pi i / 2n}
+            row[i + (i >> PS)] = cj<T>(mulc<T>(mk<T>(x.x, -x.y), t));
+          }
+        }
+      }
+    }
+    __syncthreads();
+    fx_middle<T, OP, E, COL, false, 0, NP - 1>(a, row0, rows, buf, tw, scale, pair_ok);
+    fx_pass<T, OP, E, NP - 1, COL, false, FX_SMEM, FX_GLOBAL>(a, row0, rows, buf, nullptr, tw, scale, pair_ok);
   } else {  // OP_C2R_EVEN
     // staged Hermitian load fused with the merge: the thread takes the pairs (i, L - i),
     // i = first + q * TPR <= L / 2, loads both bins (all loads issued before any use), applies

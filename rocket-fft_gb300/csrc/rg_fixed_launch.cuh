@@ -1,6 +1,6 @@
-// Launchers of the compile-time-L kernels (rg_fixed_kernel.cuh), instantiated per precision by
-// rg_fixed_f32.cu / rg_fixed_f64.cu for L = 64 ... 4096 (row walk) and L = 64 ... 1024
-// (column walk).
+// Launchers of the compile-time-L kernels (rg_fixed_kernel.cuh) for L = 64 ... 4096 (row walk)
+// and L = 64 ... 1024 (column walk); instantiated per precision and op family in
+// rg_fixed_{f32,f64}{,_real,_dct}.cu.
 #pragma once
 #include "rg_error.hpp"
 #include "rg_fixed_kernel.cuh"
@@ -38,23 +38,37 @@ bool fx_by_length(int E, const KArgs &a, int pair_ok, cudaStream_t st) {
   return false;
 }
 
+// Instances of one op (both walks and, for c2c, both directions); defined in the per-op
+// translation units so that they compile in parallel.
+template <typename T, int OP> bool launch_fixed_op(const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st);
+
+template <typename T, int OP>
+bool launch_fixed_op_impl(int E, const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st) {
+  if constexpr (OP == OP_C2C) {
+    if (col) return bwd ? fx_by_length<T, OP, true, true>(E, a, pair_ok, st) : fx_by_length<T, OP, true, false>(E, a, pair_ok, st);
+    return bwd ? fx_by_length<T, OP, false, true>(E, a, pair_ok, st) : fx_by_length<T, OP, false, false>(E, a, pair_ok, st);
+  } else {
+    return col ? fx_by_length<T, OP, true, false>(E, a, pair_ok, st) : fx_by_length<T, OP, false, false>(E, a, pair_ok, st);
+  }
+}
+
+#define RG_FIXED_OP_INSTANCE(T, OP)                                                                          \
+  template <>                                                                                                \
+  bool launch_fixed_op<T, OP>(const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st) {           \
+    int E = 0;                                                                                               \
+    while ((1 << E) < a.core.L) ++E;                                                                         \
+    if ((1 << E) != a.core.L) return false;                                                                  \
+    return launch_fixed_op_impl<T, OP>(E, a, col, bwd, pair_ok, st);                                         \
+  }
+
 // True when an instance exists for (op, L, walk, direction) and was launched.
 template <typename T> bool launch_fixed_typed(int op, const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st) {
-  int E = 0;
-  while ((1 << E) < a.core.L) ++E;
-  if ((1 << E) != a.core.L) return false;
   switch (op) {
-    case OP_C2C:
-      if (col) return bwd ? fx_by_length<T, OP_C2C, true, true>(E, a, pair_ok, st)
-                          : fx_by_length<T, OP_C2C, true, false>(E, a, pair_ok, st);
-      return bwd ? fx_by_length<T, OP_C2C, false, true>(E, a, pair_ok, st)
-                 : fx_by_length<T, OP_C2C, false, false>(E, a, pair_ok, st);
-    case OP_R2C_EVEN:
-      return col ? fx_by_length<T, OP_R2C_EVEN, true, false>(E, a, pair_ok, st)
-                 : fx_by_length<T, OP_R2C_EVEN, false, false>(E, a, pair_ok, st);
-    case OP_C2R_EVEN:
-      return col ? fx_by_length<T, OP_C2R_EVEN, true, false>(E, a, pair_ok, st)
-                 : fx_by_length<T, OP_C2R_EVEN, false, false>(E, a, pair_ok, st);
+    case OP_C2C: return launch_fixed_op<T, OP_C2C>(a, col, bwd, pair_ok, st);
+    case OP_R2C_EVEN: return launch_fixed_op<T, OP_R2C_EVEN>(a, col, bwd, pair_ok, st);
+    case OP_C2R_EVEN: return launch_fixed_op<T, OP_C2R_EVEN>(a, col, bwd, pair_ok, st);
+    case OP_DCT2: return launch_fixed_op<T, OP_DCT2>(a, col, bwd, pair_ok, st);
+    case OP_DCT3: return launch_fixed_op<T, OP_DCT3>(a, col, bwd, pair_ok, st);
     default: return false;
   }
 }

@@ -113,3 +113,28 @@ def test_stream_variants(env):
                         str(ROOT / "tests" / "test_gpu_pow2_kernels.py"), "-k", "not variants"],
                        env=e, capture_output=True, text=True, cwd=str(ROOT))
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+
+
+DCT_CASES = [
+    # shape, axes, dtype, type, cosine, ortho, fct
+    ((128, 64, 512), (0, 1, 2), np.float32, 2, True, False, 1.0),
+    ((128, 64, 512), (2, 0), np.float32, 3, True, True, 1.0),
+    ((256, 1024), (1,), np.float32, 2, False, False, 0.5),
+    ((512, 300), (0,), np.float32, 3, False, True, 1.0),
+    ((64, 64, 256), (0, 1, 2), np.float64, 2, True, True, 1.0),
+    ((2048, 128), (1, 0), np.float64, 3, False, False, 2.0),
+]
+
+
+@pytest.mark.parametrize("shape,axes,dtype,type_,cosine,ortho,fct", DCT_CASES)
+def test_stream_dct23(rg, cuda, shape, axes, dtype, type_, cosine, ortho, fct):
+    torch = cuda
+    x = _rand(shape, dtype, 4)
+    want = np.empty(shape, np.float64)
+    fn = "dct" if cosine else "dst"
+    getattr(oracle.port(), fn)(x.astype(np.float64), want, axes, type_, fct, ortho)
+    xd = torch.from_numpy(x).cuda()
+    out = torch.empty_like(xd)
+    getattr(rg, fn)(xd, out, np.array(axes, np.int64), type_, fct, ortho, 1)
+    torch.cuda.synchronize()
+    _check(out.cpu().numpy(), want, dtype)
