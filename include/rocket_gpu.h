@@ -131,18 +131,31 @@ int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, ro
  * the transform path). Grids are C-contiguous n0 x n1 x n2, h = 1, Neumann boundaries (mirrored
  * ghost cells); the DCT-II diagonalises the 7-point Laplacian with eigenvalues
  * lam0[k0] + lam1[k1] + lam2[k2], lam_a[k] = 2 cos(pi k / n_a) - 2.
- *   rocketgpu_poisson_eigdiv: X /= lambda in place (float or double, itemsize 4/8), mode 0 set
+ *   rocketgpu_poisson_eigdiv: X /= lambda in place (float or double, itemsize 4/8; the table lam =
+ *     lam0|lam1|lam2 is in the same precision as X, arithmetic in that precision), mode 0 set
  *     to 0; lam = the three device tables back to back (n0+n1+n2 doubles).
  *   rocketgpu_poisson_update: u += delta with an exact two-sum whose rounding error goes to the
  *     float u_lo (u_lo may be NULL).
  *   rocketgpu_poisson_residual: r = f - A (u + u_lo) in double (u_lo may be NULL), written as
  *     float to r32 (if not NULL); sum(r^2) to *sumsq (device).
+ *   rocketgpu_poisson_to_fx / _update_fx / _residual_fx / _fx_to_double: the same refinement
+ *     with the iterate and the right-hand side in fixed point, u = U * 2^-e, f = F * 2^-e + Frem
+ *     (U, F int64, Frem float, may be NULL): F = round(f * 2^e), Frem = f - F 2^-e;
+ *     U += round(delta * 2^e); r = 2^-e (F - A U) + Frem, exact in integers until the final
+ *     rounding to float (r32 if not NULL; sum(r^2) to *sumsq, squares formed
+ *     as (r 2^-k)^2 with k the caller's estimate of log2 max|f|); out = U * 2^-e. The caller
+ *     picks e so that |U| and |F| stay below 2^62.
  * All return a status; rocketgpu_poisson_last_error gives the calling thread's message. */
-int rocketgpu_poisson_eigdiv(void *X, int64_t itemsize, int64_t n0, int64_t n1, int64_t n2, const double *lam,
+int rocketgpu_poisson_eigdiv(void *X, int64_t itemsize, int64_t n0, int64_t n1, int64_t n2, const void *lam,
                              void *stream);
 int rocketgpu_poisson_update(double *u, float *u_lo, const float *delta, int64_t total, void *stream);
 int rocketgpu_poisson_residual(const double *u, const float *u_lo, const double *f, float *r32, int64_t n0,
                                int64_t n1, int64_t n2, double *sumsq, void *stream);
+int rocketgpu_poisson_update_fx(int64_t *U, const float *delta, int64_t total, int32_t e, void *stream);
+int rocketgpu_poisson_to_fx(const double *f, int32_t e, int64_t *F, float *Frem, int64_t total, void *stream);
+int rocketgpu_poisson_residual_fx(const int64_t *U, const int64_t *F, const float *Frem, int32_t e, int32_t k,
+                                  float *r32, int64_t n0, int64_t n1, int64_t n2, double *sumsq, void *stream);
+int rocketgpu_poisson_fx_to_double(const int64_t *U, int32_t e, double *out, int64_t total, void *stream);
 const char *rocketgpu_poisson_last_error(void);
 
 /* ---- batched uneven-length complex FFTs (no reference counterpart) ----

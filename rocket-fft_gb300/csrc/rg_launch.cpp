@@ -2,6 +2,7 @@
 #include "rg_launch.hpp"
 
 #include <atomic>
+#include <functional>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -99,6 +100,10 @@ uint64_t axis_bytes(DType dt, int op, const KArgs &a) {
 }  // namespace
 
 void profile_enable(bool on) { g_prof.store(on); }
+
+void profiled_launch(const char *name, uint64_t bytes, cudaStream_t st, const std::function<void()> &launch) {
+  timed(name, bytes, st, launch);
+}
 
 std::vector<KernelStat> profile_read() {
   std::lock_guard<std::mutex> lk(g_pmu);

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <vector>
 
 #include "rg_common.cuh"
@@ -98,6 +99,9 @@ struct KernelStat {
   uint64_t bytes = 0;
 };
 void profile_enable(bool on);
+// Run `launch` (one kernel launch on `st`) under the profile when it is enabled, recording
+// `bytes` algorithmic bytes for kernel `name`.
+void profiled_launch(const char *name, uint64_t bytes, cudaStream_t st, const std::function<void()> &launch);
 std::vector<KernelStat> profile_read();
 void profile_reset();
 

@@ -8,8 +8,10 @@
 //
 // rocketgpu_poisson_eigdiv: X_k /= lambda_k in place (DCT-II coefficients, float or double).
 // rocketgpu_poisson_update: u_hi + u_lo += delta (exact two-sum, rounding error into u_lo).
-// rocketgpu_poisson_residual: r = f - A(u_hi + u_lo) in double, written as float for the next
-//   single-precision solve, and sum(r^2).
+// rocketgpu_poisson_residual: r = f - A(u_hi + u_lo) (the u_hi stencil in double), written as
+//   float for the next single-precision solve, and sum(r^2).
+// GB300 executes FP64 at a small fraction of its FP32 rate, so each kernel keeps in double only
+// what the 1e-12 target needs: the exact u_hi differences and their sum, and u_hi itself.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,14 +30,57 @@ struct Grid {
   int64_t n0, n1, n2;
 };
 
+// Grid of the stencil-shaped kernels: x = positions along the last axis (blockDim.x threads
+// each), y = index along the middle axis, z = index along the first axis; no divisions.
+// X /= lambda in X's own precision: the float32 spectral solve of the mixed-precision
+// refinement only needs float accuracy, and GB300's FP64 rate would otherwise bound it (the
+// eigenvalues are all <= 0, so their sum has no cancellation).
 template <typename T>
-__global__ void __launch_bounds__(256) eigdiv_kernel(T *X, Grid g, const double *l0, const double *l1,
-                                                     const double *l2) {
-  const int64_t total = g.n0 * g.n1 * g.n2;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t k2 = i % g.n2, t = i / g.n2, k1 = t % g.n1, k0 = t / g.n1;
-    const double lam = l0[k0] + l1[k1] + l2[k2];
-    X[i] = i == 0 ? T(0) : T(double(X[i]) / lam);
+__global__ void __launch_bounds__(256) eigdiv_kernel(T *X, Grid g, const T *l0, const T *l1, const T *l2) {
+  const int64_t k2 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k2 >= g.n2) return;
+  const int64_t k1 = blockIdx.y, k0 = blockIdx.z;
+  const int64_t i = (k0 * g.n1 + k1) * g.n2 + k2;
+  const T lam = (l0[k0] + l1[k1]) + l2[k2];
+  X[i] = i == 0 ? T(0) : X[i] / lam;
+}
+
+// r = f - A(u_hi + u_lo): the hi second differences (a - c) + (b - c) are exact for a smooth
+// iterate (neighbours within a factor of two, Sterbenz); the lo part only needs float accuracy.
+// Neighbours come from L1/L2: a block row's planes above and below are recently read rows.
+__global__ void __launch_bounds__(256) residual_kernel(const double *uh, const float *ul, const double *f,
+                                                       float *r32, Grid g, double *sum) {
+  const int64_t k2 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t k1 = blockIdx.y, k0 = blockIdx.z;
+  const int64_t s0 = g.n1 * g.n2, s1 = g.n2;
+  double acc = 0.0;
+  if (k2 < g.n2) {
+    const int64_t i = k0 * s0 + k1 * s1 + k2;
+    // mirrored neighbours (Neumann): an out-of-range neighbour is the cell itself
+    const int64_t m0 = k0 > 0 ? i - s0 : i, p0 = k0 + 1 < g.n0 ? i + s0 : i;
+    const int64_t m1 = k1 > 0 ? i - s1 : i, p1 = k1 + 1 < g.n1 ? i + s1 : i;
+    const int64_t m2 = k2 > 0 ? i - 1 : i, p2 = k2 + 1 < g.n2 ? i + 1 : i;
+    const double c = uh[i];
+    const double Au = ((uh[m0] - c) + (uh[p0] - c)) + ((uh[m1] - c) + (uh[p1] - c)) + ((uh[m2] - c) + (uh[p2] - c));
+    // r = (f - A u_hi) - A u_lo: the second term is a small correction, float is enough for it
+    // and for the float32 copy of r
+    float r = float(f[i] - Au);
+    if (ul) {
+      const float cl = ul[i];
+      r -= ((ul[m0] - cl) + (ul[p0] - cl)) + ((ul[m1] - cl) + (ul[p1] - cl)) + ((ul[m2] - cl) + (ul[p2] - cl));
+    }
+    if (r32) r32[i] = r;
+    acc = double(r) * double(r);  // squared in double: no overflow for large right-hand sides
+  }
+  // block reduction of sum(r^2): warp shuffles, then one value per warp
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
+    atomicAdd(sum, t);
   }
 }
 
@@ -43,54 +88,95 @@ __global__ void __launch_bounds__(256) eigdiv_kernel(T *X, Grid g, const double 
 // optional): corrections are added to u_hi by an exact two-sum whose rounding error goes to u_lo,
 // so the iterate keeps more than a double's precision and the residual floor drops well below
 // the 1e-12 target (a single double leaves a floor near 1e-12 on a 512^3 grid).
-__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
-  s = a + b;
-  const double bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
+// u_hi + u_lo += delta: exact sum in double (Dekker's fast two-sum on the operands ordered by
+// magnitude, three double operations), rounding error added to u_lo in float
+__global__ void __launch_bounds__(256) update_kernel(double *uh, float *ul, const float *delta, int64_t total) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const double a = uh[i], b = double(delta[i]);
+    const double s = a + b;
+    const bool big_a = fabs(a) >= fabs(b);
+    const double e = big_a ? b - (s - a) : a - (s - b);
+    uh[i] = s;
+    if (ul) ul[i] += float(e);
+  }
 }
 
-// r = f - A(u_hi + u_lo): the hi second differences (a - c) + (b - c) are exact for a smooth
-// iterate (neighbours within a factor of two, Sterbenz); the lo part only needs float accuracy.
-__global__ void __launch_bounds__(256) residual_kernel(const double *uh, const float *ul, const double *f,
-                                                       float *r32, Grid g, double *sum) {
-  const int64_t total = g.n0 * g.n1 * g.n2;
+// ---- fixed-point iterate --------------------------------------------------------------------
+// u = U * 2^-e with U int64: the 7-point differences and their sum are exact integer arithmetic
+// (GB300 runs int64 adds on its integer pipes and FP64 at about one operation per clock per SM),
+// and only f - A u is formed in double. e is chosen from the first correction so that
+// |U| < 2^62, which keeps 2^-e at about 2^-60 of max|u| -- the residual floor this leaves is
+// well below the 1e-12 target.
+
+// U += round(delta * 2^e)
+__global__ void __launch_bounds__(256) fx_update_kernel(long long *U, const float *delta, int64_t total, int e) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
+    U[i] += __float2ll_rn(ldexpf(delta[i], e));
+}
+
+// Float of an int64 through the two 32-bit halves of its magnitude (32-bit conversions, no
+// FP64; splitting the magnitude rather than the two's-complement value avoids cancellation for
+// small negative values): exact for |v| < 2^24, within one rounding of float otherwise.
+__device__ __forceinline__ float ll_to_float(long long v) {
+  const unsigned long long m = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const unsigned hi = unsigned(m >> 32), lo = unsigned(m & 0xffffffffull);
+  const float a = hi ? fmaf(float(hi), 4294967296.0f, float(lo)) : float(lo);
+  return v < 0 ? -a : a;
+}
+
+// R = F - A U exact in int64 (F = f on the iterate's fixed-point scale), r = R 2^-e + Frem
+// written as float; sum(r^2) accumulated as sum((r 2^-k)^2) 2^2k, k from max |f|, so that float
+// squares neither overflow nor underflow.
+__global__ void __launch_bounds__(256) fx_residual_kernel(const long long *U, const long long *F, const float *Frem,
+                                                          float *r32, Grid g, int e, int k, double *sum) {
+  const int64_t k2 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t k1 = blockIdx.y, k0 = blockIdx.z;
   const int64_t s0 = g.n1 * g.n2, s1 = g.n2;
-  double acc = 0.0;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t k2 = i % g.n2, t = i / g.n2, k1 = t % g.n1, k0 = t / g.n1;
-    // mirrored neighbours (Neumann): an out-of-range neighbour is the cell itself
+  float acc = 0.f;
+  if (k2 < g.n2) {
+    const int64_t i = k0 * s0 + k1 * s1 + k2;
     const int64_t m0 = k0 > 0 ? i - s0 : i, p0 = k0 + 1 < g.n0 ? i + s0 : i;
     const int64_t m1 = k1 > 0 ? i - s1 : i, p1 = k1 + 1 < g.n1 ? i + s1 : i;
     const int64_t m2 = k2 > 0 ? i - 1 : i, p2 = k2 + 1 < g.n2 ? i + 1 : i;
-    const double c = uh[i];
-    double Au = ((uh[m0] - c) + (uh[p0] - c)) + ((uh[m1] - c) + (uh[p1] - c)) + ((uh[m2] - c) + (uh[p2] - c));
-    if (ul) {
-      const float cl = ul[i];
-      Au += double(((ul[m0] - cl) + (ul[p0] - cl)) + ((ul[m1] - cl) + (ul[p1] - cl)) + ((ul[m2] - cl) + (ul[p2] - cl)));
-    }
-    const double r = f[i] - Au;
-    if (r32) r32[i] = float(r);
-    acc += r * r;
+    // modulo-2^64 arithmetic: the intermediate sums may wrap, the result (f minus a second
+    // difference, small) is exact
+    const unsigned long long c = (unsigned long long)U[i];
+    const unsigned long long au = ((unsigned long long)U[m0] + (unsigned long long)U[p0]) +
+                                  ((unsigned long long)U[m1] + (unsigned long long)U[p1]) +
+                                  ((unsigned long long)U[m2] + (unsigned long long)U[p2]) - 6ull * c;
+    const long long R = (long long)((unsigned long long)F[i] - au);
+    // f = F 2^-e + Frem: the remainder keeps f's bits below the fixed-point grid
+    const float rf = ldexpf(ll_to_float(R), -e) + (Frem ? Frem[i] : 0.f);
+    if (r32) r32[i] = rf;
+    const float rs = ldexpf(rf, -k);
+    acc = rs * rs;
   }
-  // block reduction of sum(r^2)
-  __shared__ double red[256];
-  red[threadIdx.x] = acc;
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ float red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
+    atomicAdd(sum, std::ldexp(double(t), 2 * k));
   }
-  if (threadIdx.x == 0) atomicAdd(sum, red[0]);
 }
 
-// u_hi + u_lo += delta: exact two-sum, rounding error into u_lo
-__global__ void __launch_bounds__(256) update_kernel(double *uh, float *ul, const float *delta, int64_t total) {
+// F = round(f * 2^e), Frem = f - F 2^-e (exact in double, stored as float)
+__global__ void __launch_bounds__(256) fx_from_double_kernel(const double *f, long long *F, float *Frem, int64_t total,
+                                                             int e) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    double s, e;
-    two_sum(uh[i], double(delta[i]), s, e);
-    uh[i] = s;
-    if (ul) ul[i] = float(double(ul[i]) + e);
+    const long long v = __double2ll_rn(ldexp(f[i], e));
+    F[i] = v;
+    if (Frem) Frem[i] = float(f[i] - ldexp(double(v), -e));
   }
+}
+
+// out = U * 2^-e
+__global__ void __launch_bounds__(256) fx_to_double_kernel(const long long *U, double *out, int64_t total,
+                                                           double inv_scale) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = double(U[i]) * inv_scale;
 }
 
 thread_local std::string t_err;
@@ -114,24 +200,35 @@ unsigned grid_for(int64_t total) {
   return unsigned(std::min<int64_t>(b, 152 * 16));
 }
 
+dim3 grid3(const Grid &g) {
+  RG_CHECK(g.n1 < 65536 && g.n0 < 65536, RG_ERR_UNSUPPORTED, "grid extent beyond 65535 along the first two axes");
+  return dim3(unsigned((g.n2 + 255) / 256), unsigned(g.n1), unsigned(g.n0));
+}
+
 }  // namespace
 
 // X: C-contiguous n0 x n1 x n2 DCT-II coefficients (itemsize 4 or 8), divided in place by the
-// Neumann eigenvalues lam0[k0] + lam1[k1] + lam2[k2] (device tables, lam = lam0|lam1|lam2 with
-// lam_a[k] = 2 cos(pi k / n_a) - 2); mode (0,0,0) set to 0.
+// Neumann eigenvalues lam0[k0] + lam1[k1] + lam2[k2] (device tables in X's precision,
+// lam = lam0|lam1|lam2 with lam_a[k] = 2 cos(pi k / n_a) - 2); mode (0,0,0) set to 0.
 extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_eigdiv(void *X, int64_t itemsize, int64_t n0,
                                                                               int64_t n1, int64_t n2,
-                                                                              const double *lam, void *stream) {
+                                                                              const void *lam, void *stream) {
   return guarded([&] {
     RG_CHECK(itemsize == 4 || itemsize == 8, RG_ERR_ARG, "float32 or float64 coefficients required");
     RG_CHECK(n0 > 0 && n1 > 0 && n2 > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Grid g{n0, n1, n2};
-    const unsigned b = grid_for(n0 * n1 * n2);
-    if (itemsize == 4)
-      eigdiv_kernel<float><<<b, 256, 0, st>>>(static_cast<float *>(X), g, lam, lam + n0, lam + n0 + n1);
-    else
-      eigdiv_kernel<double><<<b, 256, 0, st>>>(static_cast<double *>(X), g, lam, lam + n0, lam + n0 + n1);
+    const dim3 b = grid3(g);
+    const uint64_t bytes = uint64_t(2 * itemsize) * uint64_t(n0 * n1 * n2);
+    rg::profiled_launch(itemsize == 4 ? "poisson_eigdiv_f32" : "poisson_eigdiv_f64", bytes, st, [&] {
+      if (itemsize == 4) {
+        const float *l = static_cast<const float *>(lam);
+        eigdiv_kernel<float><<<b, 256, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
+      } else {
+        const double *l = static_cast<const double *>(lam);
+        eigdiv_kernel<double><<<b, 256, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
+      }
+    });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
@@ -144,7 +241,9 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_update(d
   return guarded([&] {
     RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    update_kernel<<<grid_for(total), 256, 0, st>>>(u, u_lo, delta, total);
+    const uint64_t bytes = uint64_t(total) * (u_lo ? 28 : 20);
+    rg::profiled_launch("poisson_update", bytes, st,
+                        [&] { update_kernel<<<grid_for(total), 256, 0, st>>>(u, u_lo, delta, total); });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
@@ -160,7 +259,66 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_residual
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     RG_CUDA(cudaMemsetAsync(sumsq, 0, sizeof(double), st));
     Grid g{n0, n1, n2};
-    residual_kernel<<<grid_for(n0 * n1 * n2), 256, 0, st>>>(u, u_lo, f, r32, g, sumsq);
+    const uint64_t bytes = uint64_t(n0 * n1 * n2) * (16 + (u_lo ? 4 : 0) + (r32 ? 4 : 0));
+    rg::profiled_launch("poisson_residual", bytes, st,
+                        [&] { residual_kernel<<<grid3(g), 256, 0, st>>>(u, u_lo, f, r32, g, sumsq); });
+    rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+// Fixed-point iterate u = U * 2^-e (U int64, C-contiguous n0 x n1 x n2).
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_update_fx(int64_t *U, const float *delta,
+                                                                                 int64_t total, int32_t e,
+                                                                                 void *stream) {
+  return guarded([&] {
+    RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    rg::profiled_launch("poisson_update_fx", uint64_t(total) * 20, st, [&] {
+      fx_update_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<long long *>(U), delta, total, e);
+    });
+    rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_residual_fx(
+    const int64_t *U, const int64_t *F, const float *Frem, int32_t e, int32_t k, float *r32, int64_t n0, int64_t n1,
+    int64_t n2, double *sumsq, void *stream) {
+  return guarded([&] {
+    RG_CHECK(n0 > 0 && n1 > 0 && n2 > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RG_CUDA(cudaMemsetAsync(sumsq, 0, sizeof(double), st));
+    Grid g{n0, n1, n2};
+    const uint64_t bytes = uint64_t(n0 * n1 * n2) * (16 + (Frem ? 4 : 0) + (r32 ? 4 : 0));
+    rg::profiled_launch("poisson_residual_fx", bytes, st, [&] {
+      fx_residual_kernel<<<grid3(g), 256, 0, st>>>(reinterpret_cast<const long long *>(U),
+                                                   reinterpret_cast<const long long *>(F), Frem, r32, g, e, k, sumsq);
+    });
+    rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_to_fx(const double *f, int32_t e, int64_t *F,
+                                                                             float *Frem, int64_t total, void *stream) {
+  return guarded([&] {
+    RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    fx_from_double_kernel<<<grid_for(total), 256, 0, st>>>(f, reinterpret_cast<long long *>(F), Frem, total, e);
+    rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_fx_to_double(const int64_t *U, int32_t e,
+                                                                                    double *out, int64_t total,
+                                                                                    void *stream) {
+  return guarded([&] {
+    RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    fx_to_double_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<const long long *>(U), out, total,
+                                                         std::ldexp(1.0, -e));
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });

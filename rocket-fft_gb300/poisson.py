@@ -8,10 +8,19 @@ cells, f zero-mean (the constant mode is set to 0):
     u = DCT-III( DCT-II(f) / lambda ) / (8 n0 n1 n2),  lambda_k = sum_a (2 cos(pi k_a/n_a) - 2)
 
 ``solve(f, mixed=True)`` runs the transforms in float32 and refines in float64: residual
-r = f - A u by the 7-point stencil in double, correction from a float32 spectral solve of r,
-until ||r|| / ||f|| <= tol. Both forms return the zero-mean solution. The iterate is kept as a compensated pair u + u_lo (corrections
-added by an exact two-sum), since rounding u to one double alone leaves a residual floor near
-1e-12 on a 512^3 grid. ``mixed=False`` is the float64-throughout form (one solve).
+r = f - A u by the 7-point stencil, correction from a float32 spectral solve of r, until
+||r|| / ||f|| <= tol. Rounding the iterate to one double would leave a residual floor near 1e-12
+on a 512^3 grid, so it carries more bits, in one of two forms:
+
+* ``iterate="fixed"`` (default): u = U 2^-e and f ~ F 2^-e with U, F int64 and e set from the
+  first correction and max |f| (|U|, |F| < 2^62). The residual F - A U is exact integer
+  arithmetic, rounded once to float -- GB300 executes FP64 at about one operation per clock per
+  SM, so this keeps the refinement bound by memory, not by FP64. f's bits below the grid 2^-e
+  (about 2^-61 of max |u|) are kept as a float remainder added to each residual.
+* ``iterate="pair"``: a double u plus a float u_lo, corrections added by an exact two-sum, the
+  u differences in double.
+
+Both return the zero-mean solution. ``mixed=False`` is the float64-throughout form (one solve).
 """
 
 from __future__ import annotations
@@ -38,6 +47,15 @@ def _bind():
         lib.rocketgpu_poisson_update.restype = ctypes.c_int
         lib.rocketgpu_poisson_residual.restype = ctypes.c_int
         lib.rocketgpu_poisson_last_error.restype = ctypes.c_char_p
+        i64, i32 = ctypes.c_int64, ctypes.c_int32
+        lib.rocketgpu_poisson_update_fx.argtypes = [P, P, i64, i32, P]
+        lib.rocketgpu_poisson_update_fx.restype = ctypes.c_int
+        lib.rocketgpu_poisson_residual_fx.argtypes = [P, P, P, i32, i32, P, i64, i64, i64, P, P]
+        lib.rocketgpu_poisson_to_fx.argtypes = [P, i32, P, P, i64, P]
+        lib.rocketgpu_poisson_to_fx.restype = ctypes.c_int
+        lib.rocketgpu_poisson_residual_fx.restype = ctypes.c_int
+        lib.rocketgpu_poisson_fx_to_double.argtypes = [P, i32, P, i64, P]
+        lib.rocketgpu_poisson_fx_to_double.restype = ctypes.c_int
         lib._poisson_bound = True
     return lib
 
@@ -57,6 +75,7 @@ class NeumannPoisson:
         self.fct = 1.0 / (8.0 * n0 * n1 * n2)
         lam = np.concatenate([2 * np.cos(np.pi * np.arange(n) / n) - 2 for n in self.shape])
         self.lam = torch.from_numpy(lam).to(self.dev)
+        self.lam32 = self.lam.to(torch.float32)
         self.sumsq = torch.empty(1, dtype=torch.float64, device=self.dev)
         self.lib = _bind()
 
@@ -69,7 +88,8 @@ class NeumannPoisson:
         out = torch.empty_like(rhs) if out is None else out
         _pf.dct(rhs, work, AXES, 2, 1.0, False, 1)
         _check(self.lib, self.lib.rocketgpu_poisson_eigdiv(work.data_ptr(), rhs.element_size(), *self.shape,
-                                                            self.lam.data_ptr(), self._stream()))
+                                                            (self.lam32 if rhs.element_size() == 4 else self.lam).data_ptr(),
+                                                            self._stream()))
         _pf.dct(work, out, AXES, 3, self.fct, False, 1)
         return out
 
@@ -86,9 +106,10 @@ class NeumannPoisson:
             u.data_ptr(), u_lo.data_ptr() if u_lo is not None else None, delta.data_ptr(), u.numel(),
             self._stream()))
 
-    def solve(self, f, mixed=True, tol=1e-12, max_iter=30):
+    def solve(self, f, mixed=True, tol=1e-12, max_iter=30, iterate="fixed"):
         """Returns (u, info) with info = {iterations, rel_residual, history}."""
         assert f.dtype == torch.float64 and f.is_cuda and tuple(f.shape) == self.shape
+        assert iterate in ("fixed", "pair")
         f = f.contiguous()
         fnorm = float(torch.linalg.vector_norm(f).item())
         if not mixed:
@@ -96,21 +117,51 @@ class NeumannPoisson:
             u -= u.mean()
             rel = self.residual(u, f) / fnorm
             return u, {"iterations": 1, "rel_residual": rel, "history": [rel]}
-        u = torch.zeros_like(f)
-        u_lo = torch.zeros(self.shape, dtype=torch.float32, device=self.dev)  # iterate = u + u_lo
         r32 = f.to(torch.float32)
         d32 = torch.empty_like(r32)
         w32 = torch.empty_like(r32)
         hist = []
         rel = 1.0
-        for it in range(1, max_iter + 1):
-            self.spectral_solve(r32, out=d32, work=w32)
-            self.update(u, d32, u_lo)
-            rel = self.residual(u, f, r32=r32, u_lo=u_lo) / fnorm
-            hist.append(rel)
-            if rel <= tol:
-                break
-        u += u_lo.double()
+        if iterate == "pair":
+            u = torch.zeros_like(f)
+            u_lo = torch.zeros(self.shape, dtype=torch.float32, device=self.dev)  # iterate = u + u_lo
+            for _ in range(max_iter):
+                self.spectral_solve(r32, out=d32, work=w32)
+                self.update(u, d32, u_lo)
+                rel = self.residual(u, f, r32=r32, u_lo=u_lo) / fnorm
+                hist.append(rel)
+                if rel <= tol:
+                    break
+            u += u_lo.double()
+        else:
+            U = torch.zeros(self.shape, dtype=torch.int64, device=self.dev)
+            F = torch.empty_like(U)
+            Frem = torch.empty(self.shape, dtype=torch.float32, device=self.dev)
+            e = 0
+            n = U.numel()
+            fmax = float(f.abs().max().item())
+            k = int(np.frexp(fmax)[1]) if fmax > 0 else 0
+            for it in range(max_iter):
+                self.spectral_solve(r32, out=d32, work=w32)
+                if it == 0:
+                    # scale from the first correction (the solution to ~1e-3) and from f:
+                    # max |U|, |F| < 2^61
+                    m = max(float(d32.abs().max().item()), fmax)
+                    e = 61 - int(np.frexp(m)[1]) if m > 0 else 0
+                    _check(self.lib, self.lib.rocketgpu_poisson_to_fx(f.data_ptr(), e, F.data_ptr(), Frem.data_ptr(), n,
+                                                                      self._stream()))
+                _check(self.lib, self.lib.rocketgpu_poisson_update_fx(U.data_ptr(), d32.data_ptr(), n, e,
+                                                                     self._stream()))
+                _check(self.lib, self.lib.rocketgpu_poisson_residual_fx(
+                    U.data_ptr(), F.data_ptr(), Frem.data_ptr(), e, k, r32.data_ptr(), *self.shape,
+                    self.sumsq.data_ptr(),
+                    self._stream()))
+                rel = float(self.sumsq.sqrt().item()) / fnorm
+                hist.append(rel)
+                if rel <= tol:
+                    break
+            u = torch.empty_like(f)
+            _check(self.lib, self.lib.rocketgpu_poisson_fx_to_double(U.data_ptr(), e, u.data_ptr(), n, self._stream()))
         u -= u.mean()  # the solution is fixed up to a constant: return the zero-mean one
         return u, {"iterations": len(hist), "rel_residual": rel, "history": hist}
 
