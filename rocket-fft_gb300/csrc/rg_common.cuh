@@ -77,7 +77,10 @@ enum Op : int {
   OP_BLUE = 6,       // complex n -> complex n through a length-L (L >= 2n-1) convolution
   OP_DCT2 = 7, OP_DCT3 = 8, OP_DCT4_EVEN = 9, OP_DCT1 = 10, OP_DST1 = 11,
   OP_R2R_FFTPACK_R2H = 12, OP_R2R_FFTPACK_H2R = 13, OP_HARTLEY = 14,
-  OP_COUNT = 15
+  OP_DCT2_HALF = 15,  // DCT/DST-II of real n = 2L through the length-L complex FFT of the
+                      // Makhoul-ordered input (r2c) and the post-twiddle (compile-time-L only)
+  OP_DCT3_HALF = 16,  // DCT/DST-III of real n = 2L: pre-twiddled half spectrum, c2r (same)
+  OP_COUNT = 17
 };
 
 struct KArgs {

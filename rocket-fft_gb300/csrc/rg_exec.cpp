@@ -266,6 +266,17 @@ bool stream_geo(const Job &j, bool col, int stages, Geo &g) {
   }
 }
 
+bool fixed_job_ok(const Job &j) {
+  if (!(j.L >= 64 && (j.L & (j.L - 1)) == 0) || !pow2_enabled() || !fixed_enabled() || stream_enabled()) return false;
+  Side ld = j.ld, sd = j.st;
+  set_colmap(ld);
+  set_colmap(sd);
+  if (ld.colmap != sd.colmap || j.nrows >= (int64_t(1) << 31)) return false;
+  if (!set_fastdivs(ld) || !set_fastdivs(sd)) return false;
+  if (j.op == OP_C2C && j.cin != j.cout) return false;
+  return j.L <= (ld.colmap ? 1024 : 4096);
+}
+
 void run_job(const Job &j, cudaStream_t st) {
   if (j.nrows <= 0) return;
   const CoreTables &ct = get_core(j.L, j.dt);
@@ -336,7 +347,7 @@ void run_job(const Job &j, cudaStream_t st) {
   // C2C conjugating on both sides or neither
   const bool pow2L = j.L >= 2 && (j.L & (j.L - 1)) == 0 && pow2_enabled();
   const bool fixed_op = j.op == OP_C2C || j.op == OP_R2C_EVEN || j.op == OP_C2R_EVEN || j.op == OP_DCT2 ||
-                        j.op == OP_DCT3;
+                        j.op == OP_DCT3 || j.op == OP_DCT2_HALF || j.op == OP_DCT3_HALF;
   if (pow2L && !stream && fixed_enabled() && fixed_op && ld.colmap == sd.colmap &&
       j.nrows < (int64_t(1) << 31) && (j.op != OP_C2C || j.cin == j.cout) && set_fastdivs(a.ld) &&
       set_fastdivs(a.st)) {
@@ -344,7 +355,7 @@ void run_job(const Job &j, cudaStream_t st) {
     cfg.col = ld.colmap != 0;
     cfg.bwd = j.op == OP_C2C && j.cin;
     const size_t rsz = real_size(j.dt);
-    if (j.op == OP_R2C_EVEN || j.op == OP_DCT2) {
+    if (j.op == OP_R2C_EVEN || j.op == OP_DCT2 || j.op == OP_DCT2_HALF) {
       bool ok = ld.axis_stride == 1 && reinterpret_cast<uintptr_t>(j.in) % (2 * rsz) == 0;
       for (int d = 0; d < ld.nbd; ++d) ok = ok && ld.bstride[d] % 2 == 0;
       cfg.pair_ok = ok ? 1 : 0;
@@ -354,6 +365,8 @@ void run_job(const Job &j, cudaStream_t st) {
       cfg.pair_ok = ok ? 1 : 0;
     }
   }
+  RG_CHECK(cfg.fixed || (j.op != OP_DCT2_HALF && j.op != OP_DCT3_HALF), RG_ERR_INTERNAL,
+           "half-length DCT job without a fixed-length kernel");
   launch_axis(j.dt, j.op, a, cfg, st);
 }
 

@@ -47,6 +47,10 @@ struct Job {
   int flags = 0;        // fused DCT ops: bit 1 = DST
 };
 void run_job(const Job &j, cudaStream_t st);
+// True when run_job hands job j to a compile-time-length kernel instance (power-of-two L in the
+// instantiated range for its walk, both sides walking alike, 32-bit row numbers, specialised
+// kernels enabled). Ops that exist only there (OP_DCT2_HALF, OP_DCT3_HALF) need it.
+bool fixed_job_ok(const Job &j);
 
 // Complex transforms of `nrows` rows of length n (any n: on chip, four-step or Bluestein),
 // the forward core on data conjugated on load (cin) and store (cout), scaled by fct.

@@ -7,6 +7,8 @@ template <> bool launch_fixed_op<float, OP_R2C_EVEN>(const KArgs &, bool, bool, 
 template <> bool launch_fixed_op<float, OP_C2R_EVEN>(const KArgs &, bool, bool, int, cudaStream_t);
 template <> bool launch_fixed_op<float, OP_DCT2>(const KArgs &, bool, bool, int, cudaStream_t);
 template <> bool launch_fixed_op<float, OP_DCT3>(const KArgs &, bool, bool, int, cudaStream_t);
+template <> bool launch_fixed_op<float, OP_DCT2_HALF>(const KArgs &, bool, bool, int, cudaStream_t);
+template <> bool launch_fixed_op<float, OP_DCT3_HALF>(const KArgs &, bool, bool, int, cudaStream_t);
 
 bool launch_fixed_f32(int op, const KArgs &a, bool col, bool bwd, int pair_ok, cudaStream_t st) {
   return launch_fixed_typed<float>(op, a, col, bwd, pair_ok, st);

@@ -1,0 +1,8 @@
+// Single-precision instances of the compile-time-L axis kernels: DCT/DST types II and III through
+// the half-length FFT.
+#include "rg_fixed_launch.cuh"
+
+namespace rg {
+RG_FIXED_OP_INSTANCE(float, OP_DCT2_HALF)
+RG_FIXED_OP_INSTANCE(float, OP_DCT3_HALF)
+}  // namespace rg

@@ -208,6 +208,23 @@ __device__ __forceinline__ void fx_emit(const KArgs &a, uint32_t row0, int r, in
         const T y = v[k].x * fct;
         out[pos * s] = (sine && odd) ? -y : y;
       }
+    } else if constexpr (OP == OP_DCT3_HALF) {
+      // v_2i = Re F_i, v_2i+1 = -Im F_i (c2r of the half spectrum), then y_2j = v_j (j < n/2),
+      // y_2(n-1-j)+1 = v_j (j >= n/2); DST: odd outputs negated. n = 2L.
+      constexpr int N = 2 * C::L;
+      T *out = reinterpret_cast<T *>(a.out) + off;
+      const bool sine = (a.flags & 2) != 0;
+      auto put = [&](int jj, T y) {
+        const bool odd = jj >= N / 2;
+        const int pos = odd ? 2 * (N - 1 - jj) + 1 : 2 * jj;
+        out[pos * s] = (sine && odd) ? -y : y;
+      };
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int i = base + k * NS;
+        put(2 * i, v[k].x * fct);
+        put(2 * i + 1, -v[k].y * fct);
+      }
     } else if constexpr (OP == OP_C2R_EVEN) {
       // (x_2i, x_2i+1) = (Re F_i, -Im F_i) * fct
       T *out = reinterpret_cast<T *>(a.out) + off;
@@ -566,6 +583,143 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
             if (sine && i == 1) x.y *= e0;
             const cx<T> t = __ldg(tw3 + i);  // e^{-i pi i / 2n}
             row[i + (i >> PS)] = cj<T>(mulc<T>(mk<T>(x.x, -x.y), t));
+          }
+        }
+      }
+    }
+    __syncthreads();
+    fx_middle<T, OP, E, COL, false, 0, NP - 1>(a, row0, rows, buf, tw, scale, pair_ok);
+    fx_pass<T, OP, E, NP - 1, COL, false, FX_SMEM, FX_GLOBAL>(a, row0, rows, buf, nullptr, tw, scale, pair_ok);
+  } else if constexpr (OP == OP_DCT2_HALF) {
+    // y = DCT-II (DST-II) of real n = 2L: v = Makhoul order of x (v_m = x_2m, v_{n-1-m} =
+    // x_2m+1, DST: odd inputs negated) as L complex pairs z_j = (v_2j, v_2j+1); X = r2c(v) by
+    // the length-L FFT and the split; y_p = 2 Re(e^{-i pi k / 2n} X_k) fct, k = p (DCT) or n-1-p
+    // (DST), X_k = conj X_{n-k} for k > n/2; y_0 weighted e0.
+    constexpr int N = 2 * L;
+    const int64_t s = a.ld.axis_stride;
+    const bool sine = (a.flags & 2) != 0;
+    {
+      constexpr int HP = N / 2, NQ = (HP + TPR - 1) / TPR;
+      if (sr < rows) {
+        const T *p = reinterpret_cast<const T *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
+        cx<T> xv[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int m = si0 + q * TPR;
+          if (HP % TPR == 0 || m < HP) {
+            if (pair_ok) xv[q] = __ldg(reinterpret_cast<const cx<T> *>(p) + m);
+            else xv[q] = mk<T>(__ldg(p + 2 * m * s), __ldg(p + (2 * m + 1) * s));
+          }
+        }
+        T *row = reinterpret_cast<T *>(buf + sr * PITCH);
+        auto vput = [&](int i, T val) {  // v_i -> component (i & 1) of z_{i/2}
+          const int jz = i >> 1;
+          row[2 * (jz + (jz >> PS)) + (i & 1)] = val;
+        };
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int m = si0 + q * TPR;
+          if (HP % TPR == 0 || m < HP) {
+            vput(m, xv[q].x);
+            vput(N - 1 - m, sine ? -xv[q].y : xv[q].y);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    fx_middle<T, OP, E, COL, false, 0, NP>(a, row0, rows, buf, tw, scale, pair_ok);
+    // split Z_0..Z_{L-1} into X_0..X_L in place
+    {
+      const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux2);
+      constexpr int HALF = L / 2 + 1;
+      for (int e = tid; e < rows * HALF; e += NT) {
+        const int r = e / HALF;
+        const int k = e - r * HALF;
+        cx<T> *row = buf + r * PITCH;
+        if (k == 0) {
+          const cx<T> z0 = row[0];
+          row[0] = mk<T>(z0.x + z0.y, T(0));
+          row[L + (L >> PS)] = mk<T>(z0.x - z0.y, T(0));
+        } else {
+          const int kc = L - k;
+          const cx<T> zk = row[k + (k >> PS)], zc = cj<T>(row[kc + (kc >> PS)]);
+          const cx<T> Ev = scl<T>(add<T>(zk, zc), T(0.5));
+          const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
+          const cx<T> u = mul<T>(__ldg(w + k), O);
+          row[k + (k >> PS)] = add<T>(Ev, u);
+          if (kc != k) row[kc + (kc >> PS)] = cj<T>(sub<T>(Ev, u));
+        }
+      }
+    }
+    __syncthreads();
+    // post-twiddle and store
+    {
+      constexpr int NQ = (N + TPR - 1) / TPR;
+      const int64_t so = a.st.axis_stride;
+      const T fct = T(a.fct), e0 = T(a.e0);
+      const cx<T> *t2 = reinterpret_cast<const cx<T> *>(a.aux);  // e^{-i pi k / 2n}, k < n
+      if (sr < rows) {
+        T *p = reinterpret_cast<T *>(a.out) + side_offset32(a.st, row0 + uint32_t(sr));
+        const cx<T> *row = buf + sr * PITCH;
+#pragma unroll 4
+        for (int q = 0; q < NQ; ++q) {
+          const int pos = si0 + q * TPR;
+          if (N % TPR == 0 || pos < N) {
+            const int kk = sine ? N - 1 - pos : pos;
+            const int kx = kk <= L ? kk : N - kk;
+            cx<T> X = row[kx + (kx >> PS)];
+            if (kk > L) X.y = -X.y;
+            const cx<T> t = __ldg(t2 + kk);
+            T y = T(2) * (X.x * t.x - X.y * t.y) * fct;
+            if (pos == 0) y *= e0;
+            p[pos * so] = y;
+          }
+        }
+      }
+    }
+  } else if constexpr (OP == OP_DCT3_HALF) {
+    // y = DCT-III (DST-III) of real n = 2L: V_k = (x''_k - i x''_{n-k}) e^{i pi k / 2n} for
+    // k = 0..L (x''_q = x_q (DCT) or x_{n-1-q} (DST), x''_n = 0, input element 0 weighted e0)
+    // is the half spectrum of the real sequence v; the fused load builds V_i and V_{L-i} and
+    // merges them into conj(Z) (as C2R_EVEN, no conjugation), the passes and the last store
+    // give v and its DCT order.
+    constexpr int N = 2 * L;
+    constexpr int HP = L / 2 + 1;
+    constexpr int NQ = (HP + TPR - 1) / TPR;
+    const bool sine = (a.flags & 2) != 0;
+    if (sr < rows) {
+      const int64_t s = a.ld.axis_stride;
+      const T *p = reinterpret_cast<const T *>(a.in) + side_offset32(a.ld, row0 + uint32_t(sr));
+      const cx<T> *t2 = reinterpret_cast<const cx<T> *>(a.aux);   // e^{-i pi k / 2n}
+      const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux2);   // e^{-2 pi i k / n}
+      const T e0 = T(a.e0);
+      auto xdd = [&](int q) -> T {  // x''_q
+        if (q >= N) return T(0);
+        const int src = sine ? N - 1 - q : q;
+        T v = __ldg(p + src * s);
+        if (src == 0) v *= e0;
+        return v;
+      };
+      auto V = [&](int k) {  // conj(t_k) (x''_k - i x''_{n-k}); imaginary part of bins 0, L zeroed
+        const cx<T> t = __ldg(t2 + k);
+        cx<T> r = mulc<T>(mk<T>(xdd(k), -xdd(N - k)), t);
+        if (k == 0 || k == L) r.y = T(0);
+        return r;
+      };
+      cx<T> *row = buf + sr * PITCH;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int i = si0 + q * TPR;
+        if (HP % TPR == 0 || i < HP) {
+          const cx<T> x = V(i), y = V(L - i);
+          const cx<T> A = add<T>(x, cj<T>(y)), B = sub<T>(x, cj<T>(y));
+          if (i == 0) {
+            row[0] = cj<T>(add<T>(A, mposi<T>(B)));
+          } else {
+            const int kc = L - i;
+            const cx<T> U = mposi<T>(mulc<T>(B, __ldg(w + i)));
+            row[i + (i >> PS)] = cj<T>(add<T>(A, U));
+            if (kc != i) row[kc + (kc >> PS)] = sub<T>(A, U);
           }
         }
       }

@@ -69,6 +69,8 @@ template <typename T> bool launch_fixed_typed(int op, const KArgs &a, bool col, 
     case OP_C2R_EVEN: return launch_fixed_op<T, OP_C2R_EVEN>(a, col, bwd, pair_ok, st);
     case OP_DCT2: return launch_fixed_op<T, OP_DCT2>(a, col, bwd, pair_ok, st);
     case OP_DCT3: return launch_fixed_op<T, OP_DCT3>(a, col, bwd, pair_ok, st);
+    case OP_DCT2_HALF: return launch_fixed_op<T, OP_DCT2_HALF>(a, col, bwd, pair_ok, st);
+    case OP_DCT3_HALF: return launch_fixed_op<T, OP_DCT3_HALF>(a, col, bwd, pair_ok, st);
     default: return false;
   }
 }

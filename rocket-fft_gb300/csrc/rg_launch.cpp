@@ -59,6 +59,8 @@ const char *axis_name(int op) {
     case OP_BLUE: return "axis_bluestein";
     case OP_DCT2: return "axis_dct2";
     case OP_DCT3: return "axis_dct3";
+    case OP_DCT2_HALF: return "axis_dct2_half";
+    case OP_DCT3_HALF: return "axis_dct3_half";
     default: return "axis_other";
   }
 }
@@ -93,8 +95,9 @@ template <class F> void timed(const std::string &name, uint64_t bytes, cudaStrea
 uint64_t axis_bytes(DType dt, int op, const KArgs &a) {
   const uint64_t c = cx_size(dt), r = real_size(dt);
   // units: real pairs for the even-length real ops, single reals for the odd ones
-  const uint64_t in_unit = op == OP_R2C_EVEN ? 2 * r : (op == OP_R2C_ODD || op == OP_DCT2 || op == OP_DCT3) ? r : c;
-  const uint64_t out_unit = op == OP_C2R_EVEN ? 2 * r : (op == OP_C2R_ODD || op == OP_DCT2 || op == OP_DCT3) ? r : c;
+  const bool real_io = op == OP_DCT2 || op == OP_DCT3 || op == OP_DCT2_HALF || op == OP_DCT3_HALF;
+  const uint64_t in_unit = op == OP_R2C_EVEN ? 2 * r : (op == OP_R2C_ODD || real_io) ? r : c;
+  const uint64_t out_unit = op == OP_C2R_EVEN ? 2 * r : (op == OP_C2R_ODD || real_io) ? r : c;
   return uint64_t(a.nrows) * (uint64_t(a.nin) * in_unit + uint64_t(a.nout) * out_unit);
 }
 }  // namespace

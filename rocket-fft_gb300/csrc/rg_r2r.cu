@@ -238,6 +238,32 @@ void r2r_axis(DType dt, int K, int64_t n, const void *in, const Side &ld, void *
   if (K == K_DCT4) M = 2 * n;
   RG_CHECK(M >= 1, RG_ERR_ARG, "zero-length FFT requested");
   RG_CHECK(M < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "transform length too large");
+  if ((K == K_DCT2 || K == K_DCT3) && fused_enabled() && n % 2 == 0) {
+    // one kernel, the reference's reduction (T_dcst23, rocket_fft/_pocketfft_hdronly.h:2987-3061:
+    // a real FFT of the reordered input) on the half-length complex FFT: Makhoul reordering +
+    // r2c split + post-twiddle (type II), pre-twiddled half spectrum + c2r merge + reordering
+    // (type III); only compile-time-length kernels implement it
+    detail::Job j{};
+    j.dt = dt;
+    j.op = K == K_DCT2 ? OP_DCT2_HALF : OP_DCT3_HALF;
+    j.n = j.nin = j.nout = int(n);
+    j.L = int(n / 2);
+    j.Lsm = j.L + 1;
+    j.in = in;
+    j.out = out;
+    j.ld = ld;
+    j.st = sd;
+    j.nrows = nrows;
+    j.fct = fct;
+    j.e0 = e0;
+    j.flags = cosine ? 0 : 2;
+    if (detail::fixed_job_ok(j)) {
+      j.aux = get_roots(uint64_t(4 * n), uint64_t(n), dt);
+      j.aux2 = get_roots(uint64_t(n), uint64_t(n / 4 + 1), dt);
+      detail::run_job(j, st);
+      return;
+    }
+  }
   if ((K == K_DCT2 || K == K_DCT3) && fused_enabled() && detail::fits_core(n, dt)) {
     // one kernel: the reordering / twiddles of the reduction fused into the on-chip FFT's load
     // and store phases
