@@ -83,19 +83,37 @@ template <typename T> struct K {
   }
 
   // rows x len complex elements from global (row r at base + r*rstride + i*estride) into
-  // shared buffer s0, optionally conjugated, optionally times conj(bk[i]) (i < n) / zero beyond
+  // shared buffer s0, optionally conjugated, optionally times conj(bk[i]) (i < n) / zero beyond.
+  // Each thread issues kBatch loads before its first shared store, so that kBatch loads per
+  // thread are in flight (one at a time leaves the pass bound by memory latency).
+  static constexpr int kBatch = 8;
   __device__ void load(const cx<T> *base, int rows, int len, int64_t rstride, int64_t estride, bool conj_in,
                        const cx<T> *bk = nullptr, int nvalid = 1 << 30) {
     const int total = rows * len;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-      const int r = e / len, i = e - r * len;
-      cx<T> v = mk<T>(T(0), T(0));
-      if (i < nvalid) {
-        v = base[r * rstride + i * estride];
-        if (conj_in) v.y = -v.y;
-        if (bk) v = mulc<T>(v, bk[i]);
+    const int nth = blockDim.x;
+    for (int e0 = threadIdx.x; e0 < total; e0 += nth * kBatch) {
+      cx<T> v[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * nth;
+        v[u] = mk<T>(T(0), T(0));
+        if (e < total) {
+          const int r = e / len, i = e - r * len;
+          if (i < nvalid) {
+            v[u] = base[r * rstride + i * estride];
+            if (conj_in) v[u].y = -v[u].y;
+            if (bk) v[u] = mulc<T>(v[u], bk[i]);
+          }
+        }
       }
-      s0[sidx(r, i, pitch, a.ps)] = v;
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * nth;
+        if (e < total) {
+          const int r = e / len, i = e - r * len;
+          s0[sidx(r, i, pitch, a.ps)] = v[u];
+        }
+      }
     }
     __syncthreads();
   }
@@ -103,13 +121,21 @@ template <typename T> struct K {
   __device__ cx<T> *fft(int rows, const FFTCore &core) { return fft_rows<T>(s0, s1, rows, pitch, a.ps, core); }
 
   // rows x len from shared `res` to global (row r at base + r*rstride + i*estride); optional
-  // four-step twiddle W_N^{(col0 + r) * i}; optional conj/fct; optional *bk (y = conj(F*bk))
+  // four-step twiddle W_N^{(col0 + r) * i}; optional conj/fct; optional *bk (y = conj(F*bk)).
+  // colwalk: consecutive threads take consecutive rows (rows adjacent in memory, rstride 1).
   __device__ void store(const cx<T> *res, cx<T> *base, int rows, int len, int64_t rstride, int64_t estride,
                         bool conj_out, T scale, const cx<T> *lo = nullptr, const cx<T> *hi = nullptr, int shift = 0,
-                        int col0 = 0, const cx<T> *bk = nullptr, int nvalid = 1 << 30) {
+                        int col0 = 0, const cx<T> *bk = nullptr, int nvalid = 1 << 30, bool colwalk = false) {
     const int total = rows * len;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
-      const int r = e / len, i = e - r * len;
+      int r, i;
+      if (colwalk) {
+        i = e / rows;
+        r = e - i * rows;
+      } else {
+        r = e / len;
+        i = e - r * len;
+      }
       if (i >= nvalid) continue;
       cx<T> v = res[sidx(r, i, pitch, a.ps)];
       if (lo) v = mul<T>(v, split_twiddle<T>(lo, hi, shift, uint32_t(col0 + r) * uint32_t(i)));
@@ -132,20 +158,37 @@ template <typename T> struct K {
       // column j2 = c0 + r: elements j1 at src[j1 * n2 + j2]; Bluestein chirp/padding uses the
       // global index j = j1 * n2 + j2
       const int total = rows * n1;
-      for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int r = e / n1, j1 = e - r * n1;
-        const int j = j1 * n2 + c0 + r;
-        cx<T> v = mk<T>(T(0), T(0));
-        if (j < nvalid_in) {
-          v = src[j];
-          if (conj_in) v.y = -v.y;
-          if (bk_in) v = mulc<T>(v, bk_in[j]);
+      const int nth = blockDim.x;
+      for (int e0 = threadIdx.x; e0 < total; e0 += nth * kBatch) {
+        // columns fastest: consecutive threads read consecutive j2 of one j1 (coalesced); kBatch
+        // loads per thread in flight before the shared stores
+        cx<T> v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * nth;
+          v[u] = mk<T>(T(0), T(0));
+          if (e < total) {
+            const int j1 = e / rows, r = e - j1 * rows;
+            const int j = j1 * n2 + c0 + r;
+            if (j < nvalid_in) {
+              v[u] = src[j];
+              if (conj_in) v[u].y = -v[u].y;
+              if (bk_in) v[u] = mulc<T>(v[u], bk_in[j]);
+            }
+          }
         }
-        s0[sidx(r, j1, pitch, a.ps)] = v;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * nth;
+          if (e < total) {
+            const int j1 = e / rows, r = e - j1 * rows;
+            s0[sidx(r, j1, pitch, a.ps)] = v[u];
+          }
+        }
       }
       __syncthreads();
       cx<T> *res = fft(rows, c1);
-      store(res, tmp + c0, rows, n1, 1, n2, false, T(1), lo, hi, shift, c0);
+      store(res, tmp + c0, rows, n1, 1, n2, false, T(1), lo, hi, shift, c0, nullptr, 1 << 30, true);
     }
     __syncthreads();
     const int tbB = rows_for(n2);
@@ -153,7 +196,7 @@ template <typename T> struct K {
       const int rows = min(tbB, n1 - k0);
       load(tmp + int64_t(k0) * n2, rows, n2, n2, 1, false);
       cx<T> *res = fft(rows, c2);
-      store(res, dst + k0, rows, n2, 1, n1, conj_out, scale);
+      store(res, dst + k0, rows, n2, 1, n1, conj_out, scale, nullptr, nullptr, 0, 0, nullptr, 1 << 30, true);
     }
   }
 };
@@ -207,10 +250,12 @@ __global__ void __launch_bounds__(512) batch_kernel(const __grid_constant__ Batc
       cx<T> *A = w, *B = w + I.m;
       k.four_step(x, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, k.bwd, false, T(1), bk, I.n);
       __syncthreads();
+#pragma unroll 4
       for (int i = threadIdx.x; i < I.m; i += blockDim.x) A[i] = cj<T>(mul<T>(A[i], bkf[i]));
       __syncthreads();
       k.four_step(A, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, false, false, T(1));
       __syncthreads();
+#pragma unroll 4
       for (int i = threadIdx.x; i < I.n; i += blockDim.x) {
         cx<T> v = cj<T>(mul<T>(A[i], bk[i]));
         y[i] = mk<T>(v.x * k.fct, (k.bwd ? -v.y : v.y) * k.fct);
