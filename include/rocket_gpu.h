@@ -241,6 +241,14 @@ int rocketgpu_set_tc_split(int on);
 int rocketgpu_tc_error(void *stream);
 int rocketgpu_tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D, void *stream);
 
+/* N-d cyclic shift, numpy.roll semantics over every dimension: out[(i_d + shifts[d]) mod n_d] =
+ * in[i_d] (shifts: host array of ndim entries, any sign). The fftshift/ifftshift helpers of the
+ * reference's NumPy/SciPy layer (rocket_fft/overloads.py:1251-1310, via np.roll). Any element
+ * size of 1-16 bytes; in and out must be distinct arrays of the same shape; device arrays in
+ * place, host arrays staged. Returns a status. */
+int rocketgpu_roll(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                   const int64_t *shifts);
+
 /* Library version string. */
 const char *rocketgpu_version(void);
 

@@ -29,11 +29,14 @@ from .pocketfft import (  # noqa: F401
     r2r_fftpack,
     r2r_genuine_hartley,
     r2r_separable_hartley,
+    roll,
     set_stream,
     set_tc_split,
     tc_error,
     tc_selftest,
     version,
 )
+
+from . import fft, numpy_fft  # noqa: F401,E402  (SciPy/NumPy-level front ends)
 
 __version__ = "0.1.0"

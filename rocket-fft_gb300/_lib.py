@@ -88,6 +88,8 @@ def _declare(lib):
     lib.rocketgpu_profile_read.argtypes = [ctypes.POINTER(KStat), ctypes.c_int]
     lib.rocketgpu_profile_read.restype = i32
     lib.rocketgpu_profile_reset.restype = None
+    lib.rocketgpu_roll.argtypes = [u64, P, P, ctypes.POINTER(ctypes.c_int64)]
+    lib.rocketgpu_roll.restype = i32
     lib.rocketgpu_set_tc_split.argtypes = [i32]
     lib.rocketgpu_set_tc_split.restype = i32
     lib.rocketgpu_tc_error.argtypes = [P]

@@ -494,6 +494,21 @@ RG_EXPORT uint64_t rocketgpu_launch_count(void) { return rg::launch_count(); }
 
 RG_EXPORT int rocketgpu_set_tc_split(int on) { return rg::set_tc_split(on != 0); }
 
+RG_EXPORT int rocketgpu_roll(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
+                             const int64_t *shifts) {
+  return guarded([&] {
+    const Desc din = parse(ndim, ain, "ain"), dout = parse(ndim, aout, "aout");
+    RG_CHECK(din.itemsize == dout.itemsize, RG_ERR_ARG, "input and output dtypes differ");
+    check_same_shape(din, dout);
+    RG_CHECK(shifts != nullptr || ndim == 0, RG_ERR_ARG, "shifts is NULL");
+    if (any_zero(din.shape)) return;
+    const std::vector<int64_t> sh(shifts, shifts + ndim);
+    with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
+      rg::roll(i, o, din.itemsize, sh, st);
+    });
+  });
+}
+
 RG_EXPORT int rocketgpu_tc_error(void *stream) {
   int flag = 0;
   const int st = guarded([&] { flag = rg::tc_error_flag(static_cast<cudaStream_t>(stream)); });

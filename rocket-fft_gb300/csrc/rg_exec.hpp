@@ -42,6 +42,11 @@ void exec_r2r_fftpack(DType dt, const NdArray &in, const NdArray &out, const Axe
 void exec_hartley(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool genuine, double fct,
                   cudaStream_t st);
 
+// out = in cyclically shifted by shifts[d] along every dimension d (rg_shift.cu); element size
+// 1, 2, 4, 8 or 16 bytes; in and out distinct.
+void roll(const NdArray &in, const NdArray &out, int64_t itemsize, const std::vector<int64_t> &shifts,
+          cudaStream_t st);
+
 // Device workspace from a per-device stream-ordered pool.
 class DevBuf {
  public:

@@ -1,0 +1,498 @@
+"""SciPy/NumPy-level FFT front end on the GPU transform path.
+
+The functions of ``scipy.fft`` (and, in :mod:`numpy_fft`, of ``numpy.fft``) that rocket-fft
+overloads for Numba (``rocket_fft/overloads.py``), for torch tensors on the GPU (and CPU torch
+tensors or NumPy arrays, which the library stages through the GPU): every transform runs in the
+library's kernels through the low-level calls of :mod:`pocketfft`. Argument handling follows
+the reference's front end:
+
+* ``s``/``n`` and ``axes``: ``ndshape_and_axes`` (overloads.py:436-489) -- negative axes wrap,
+  ``s`` without ``axes`` takes the last ``len(s)`` axes, SciPy rejects repeated axes
+  (overloads.py:387-394; NumPy allows them);
+* the input is zero-padded or cropped to ``s`` and cast to the transform's precision
+  (``zeropad_or_crop``, overloads.py:574-607): float32/complex64 stay single precision, other
+  real or integer types become float64/complex128;
+* ``norm`` -> ``fct`` (``get_fct``/``mul_axes``, overloads.py:492-551), with the DCT/DST length
+  N = 2 (n + delta), delta = -1 for DCT-I, +1 for DST-I, 0 otherwise;
+* inverse DCT/DST swap types 2 and 3 (``get_type``, overloads.py:680-712); ``orthogonalize``
+  defaults to ``norm == "ortho"`` (``get_ortho``, overloads.py:715-732);
+* ``fft`` of real input is ``c2c_sym``; ``hfft`` is ``c2r`` with ``forward=True`` and ``ihfft``
+  ``r2c`` with ``forward=False`` (overloads.py:1488-1571); complex input to a DCT/DST transforms
+  the real and imaginary parts separately (overloads.py:991-1020).
+
+``workers`` is validated as in the reference and otherwise unused (the GPU grid replaces the
+thread pool); ``plan`` is accepted and ignored.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import pocketfft as _pf
+
+try:
+    import torch as _torch
+except ImportError:  # pragma: no cover - torch is optional for NumPy callers
+    _torch = None
+
+__all__ = [
+    "fft", "ifft", "fft2", "ifft2", "fftn", "ifftn", "rfft", "irfft", "rfft2", "irfft2", "rfftn",
+    "irfftn", "hfft", "ihfft", "hfft2", "ihfft2", "hfftn", "ihfftn", "dct", "idct", "dctn", "idctn",
+    "dst", "idst", "dstn", "idstn", "fftfreq", "rfftfreq", "fftshift", "ifftshift", "next_fast_len",
+]
+
+
+# ---------------------------------------------------------------------------------------------
+# array helpers (torch tensors and NumPy arrays)
+# ---------------------------------------------------------------------------------------------
+
+def _is_torch(x):
+    return _torch is not None and isinstance(x, _torch.Tensor)
+
+
+def _asarray(x):
+    if _is_torch(x) or isinstance(x, np.ndarray):
+        return x
+    if hasattr(x, "__cuda_array_interface__") and _torch is not None:
+        return _torch.as_tensor(x, device="cuda")
+    return np.asarray(x)
+
+
+def _kind(x):
+    """'c' complex, 'f' float, 'i' integer/bool."""
+    if _is_torch(x):
+        return "c" if x.is_complex() else ("f" if x.is_floating_point() else "i")
+    return {"c": "c", "f": "f"}.get(x.dtype.kind, "i")
+
+
+def _single(x):
+    if _is_torch(x):
+        return x.dtype in (_torch.float32, _torch.complex64, _torch.float16, _torch.bfloat16)
+    return x.dtype in (np.float32, np.complex64, np.float16)
+
+
+def _dtype(x, complex_):
+    single = _single(x)
+    if _is_torch(x):
+        if complex_:
+            return _torch.complex64 if single else _torch.complex128
+        return _torch.float32 if single else _torch.float64
+    if complex_:
+        return np.complex64 if single else np.complex128
+    return np.float32 if single else np.float64
+
+
+def _cast(x, dtype):
+    if _is_torch(x):
+        return x if x.dtype == dtype else x.to(dtype)
+    return x if x.dtype == dtype else x.astype(dtype)
+
+
+def _empty(like, shape, dtype):
+    if _is_torch(like):
+        return _torch.empty(tuple(shape), dtype=dtype, device=like.device)
+    return np.empty(tuple(shape), dtype=dtype)
+
+
+def _zeros(like, shape, dtype):
+    if _is_torch(like):
+        return _torch.zeros(tuple(shape), dtype=dtype, device=like.device)
+    return np.zeros(tuple(shape), dtype=dtype)
+
+
+def _resize(x, shape):
+    """Zero-pad or crop x to `shape` (leading corner kept)."""
+    if tuple(x.shape) == tuple(shape):
+        return x
+    out = _zeros(x, shape, x.dtype)
+    sl = tuple(slice(0, min(a, b)) for a, b in zip(x.shape, shape))
+    out[sl] = x[sl]
+    return out
+
+
+def _real_imag(x):
+    if _is_torch(x):
+        return x.real, x.imag
+    return x.real, x.imag
+
+
+# ---------------------------------------------------------------------------------------------
+# argument normalisation (rocket_fft/overloads.py:380-551, 680-732)
+# ---------------------------------------------------------------------------------------------
+
+def _axis_error(msg):
+    err = getattr(np, "exceptions", np)
+    return getattr(err, "AxisError", ValueError)(msg)
+
+
+def _wrap_axis(ax, ndim):
+    ax = int(ax)
+    if not -ndim <= ax < ndim:
+        raise _axis_error(f"axis {ax} is out of bounds for array of dimension {ndim}")
+    return ax + ndim if ax < 0 else ax
+
+
+def _shape_and_axes(x, s, axes, unique=True):
+    ndim = x.ndim
+    if s is not None:
+        s = [int(v) for v in np.atleast_1d(np.asarray(s, dtype=np.int64))]
+        for v in s:
+            if v < 1:
+                raise ValueError("Invalid number of data points specified.")
+    if axes is None:
+        if s is None:
+            axes = list(range(ndim))
+        else:
+            if len(s) > ndim:
+                raise ValueError("Shape requires more axes than are present.")
+            axes = list(range(ndim - len(s), ndim))
+    else:
+        axes = [_wrap_axis(a, ndim) for a in np.atleast_1d(np.asarray(axes, dtype=np.int64))]
+    if unique and len(set(axes)) != len(axes):
+        raise ValueError("All axes must be unique.")
+    if s is not None and len(s) != len(axes):
+        raise ValueError("When given, axes and shape arguments have to be of the same length.")
+    return s, axes
+
+
+def _one_axis(n, axis):
+    return (None if n is None else [n]), [axis]
+
+
+def _mul_axes(shape, axes, delta=None):
+    n = 1.0
+    for ax in axes:
+        n *= float(shape[ax]) if delta is None else 2.0 * (shape[ax] + delta)
+    return n
+
+
+def _fct(shape, axes, norm, forward, delta=None):
+    if norm is None or norm == "backward":
+        return 1.0 if forward else 1.0 / _mul_axes(shape, axes, delta)
+    if norm == "ortho":
+        return 1.0 / math.sqrt(_mul_axes(shape, axes, delta))
+    if norm == "forward":
+        return 1.0 / _mul_axes(shape, axes, delta) if forward else 1.0
+    raise ValueError("Invalid norm value; should be 'backward', 'ortho' or 'forward'.")
+
+
+def _check_workers(workers):
+    if workers is None:
+        return
+    w = int(workers)
+    if w == 0:
+        raise ValueError("Workers must not be zero.")
+    if w < -(__import__("os").cpu_count() or 1):
+        raise ValueError("Workers value out of range.")
+
+
+def _dct_type(type, forward):
+    type = int(type)
+    if type not in (1, 2, 3, 4):
+        raise ValueError("Invalid type; must be one of (1, 2, 3, 4).")
+    if not forward and type in (2, 3):
+        return 5 - type
+    return type
+
+
+def _axes_arg(axes):
+    return np.asarray(axes, dtype=np.int64)
+
+
+# ---------------------------------------------------------------------------------------------
+# generic transforms (rocket_fft/overloads.py:943-1045)
+# ---------------------------------------------------------------------------------------------
+
+def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=True):
+    x = _asarray(x)
+    s, axes = _shape_and_axes(x, s, axes, unique)
+    shape = list(x.shape)
+    if s is not None:
+        for n, ax in zip(s, axes):
+            shape[ax] = n
+    cdt = _dtype(x, True)
+    if _kind(x) == "c":
+        xin = _resize(_cast(x, cdt), shape)
+        out = xin if (overwrite_x or xin is not x) else _empty(xin, shape, cdt)
+        fct = _fct(shape, axes, norm, forward)
+        _pf.c2c(xin, out, _axes_arg(axes), forward, fct, 1)
+        return out
+    xin = _resize(_cast(x, _dtype(x, False)), shape)
+    out = _empty(xin, shape, cdt)
+    fct = _fct(shape, axes, norm, forward)
+    _pf.c2c_sym(xin, out, _axes_arg(axes), forward, fct, 1)
+    return out
+
+
+def _r2cn(x, s, axes, norm, forward, unique=True):
+    x = _asarray(x)
+    if _kind(x) == "c":
+        raise TypeError("x must be a real sequence")
+    s, axes = _shape_and_axes(x, s, axes, unique)
+    shape = list(x.shape)
+    if s is not None:
+        for n, ax in zip(s, axes):
+            shape[ax] = n
+    xin = _resize(_cast(x, _dtype(x, False)), shape)
+    oshape = list(shape)
+    oshape[axes[-1]] = shape[axes[-1]] // 2 + 1
+    out = _empty(xin, oshape, _dtype(x, True))
+    fct = _fct(shape, axes, norm, forward)
+    _pf.r2c(xin, out, _axes_arg(axes), forward, fct, 1)
+    return out
+
+
+def _c2rn(x, s, axes, norm, forward, unique=True):
+    x = _asarray(x)
+    s, axes = _shape_and_axes(x, s, axes, unique)
+    last = axes[-1]
+    oshape = list(x.shape)
+    oshape[last] = 2 * (x.shape[last] - 1)
+    if s is not None:
+        for n, ax in zip(s, axes):
+            oshape[ax] = n
+    if oshape[last] < 1:
+        raise ValueError(f"Invalid number of data points ({oshape[last]}) specified")
+    ishape = list(oshape)
+    ishape[last] = oshape[last] // 2 + 1
+    xin = _resize(_cast(x, _dtype(x, True)), ishape)
+    out = _empty(xin, oshape, _dtype(x, False))
+    fct = _fct(oshape, axes, norm, forward)
+    _pf.c2r(xin, out, _axes_arg(axes), forward, fct, 1)
+    return out
+
+
+def _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, forward, cosine):
+    x = _asarray(x)
+    s, axes = _shape_and_axes(x, s, axes)
+    shape = list(x.shape)
+    if s is not None:
+        for n, ax in zip(s, axes):
+            shape[ax] = n
+    type = _dct_type(type, forward)
+    delta = (-1.0 if cosine else 1.0) if type == 1 else 0.0
+    fct = _fct(shape, axes, norm, forward, delta)
+    ortho = bool(orthogonalize) if orthogonalize is not None else norm == "ortho"
+    fn = _pf.dct if cosine else _pf.dst
+    complex_ = _kind(x) == "c"
+    dt = _dtype(x, complex_)
+    xin = _resize(_cast(x, dt), shape)
+    out = xin if (overwrite_x or xin is not x) else _empty(xin, shape, dt)
+    ax = _axes_arg(axes)
+    if complex_:
+        (xr, xi), (orr, oi) = _real_imag(xin), _real_imag(out)
+        if out is xin:
+            # in place: the library transforms each part in place
+            fn(xr, xr, ax, type, fct, ortho, 1)
+            fn(xi, xi, ax, type, fct, ortho, 1)
+        else:
+            fn(xr, orr, ax, type, fct, ortho, 1)
+            fn(xi, oi, ax, type, fct, ortho, 1)
+    else:
+        fn(xin, out, ax, type, fct, ortho, 1)
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# scipy.fft
+# ---------------------------------------------------------------------------------------------
+
+def fft(x, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _c2cn(x, s, axes, norm, overwrite_x, True)
+
+
+def ifft(x, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _c2cn(x, s, axes, norm, overwrite_x, False)
+
+
+def fft2(x, s=None, axes=(-2, -1), norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2cn(x, s, axes, norm, overwrite_x, True)
+
+
+def ifft2(x, s=None, axes=(-2, -1), norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2cn(x, s, axes, norm, overwrite_x, False)
+
+
+def fftn(x, s=None, axes=None, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2cn(x, s, axes, norm, overwrite_x, True)
+
+
+def ifftn(x, s=None, axes=None, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2cn(x, s, axes, norm, overwrite_x, False)
+
+
+def rfft(x, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _r2cn(x, s, axes, norm, True)
+
+
+def irfft(x, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _c2rn(x, s, axes, norm, False)
+
+
+def rfft2(x, s=None, axes=(-2, -1), norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _r2cn(x, s, axes, norm, True)
+
+
+def irfft2(x, s=None, axes=(-2, -1), norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2rn(x, s, axes, norm, False)
+
+
+def rfftn(x, s=None, axes=None, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _r2cn(x, s, axes, norm, True)
+
+
+def irfftn(x, s=None, axes=None, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2rn(x, s, axes, norm, False)
+
+
+def hfft(x, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _c2rn(x, s, axes, norm, True)
+
+
+def ihfft(x, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _r2cn(x, s, axes, norm, False)
+
+
+def hfft2(x, s=None, axes=(-2, -1), norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2rn(x, s, axes, norm, True)
+
+
+def ihfft2(x, s=None, axes=(-2, -1), norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _r2cn(x, s, axes, norm, False)
+
+
+def hfftn(x, s=None, axes=None, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _c2rn(x, s, axes, norm, True)
+
+
+def ihfftn(x, s=None, axes=None, norm=None, overwrite_x=False, workers=None, plan=None):
+    _check_workers(workers)
+    return _r2cn(x, s, axes, norm, False)
+
+
+def dct(x, type=2, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, True, True)
+
+
+def idct(x, type=2, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, False, True)
+
+
+def dctn(x, type=2, s=None, axes=None, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, True, True)
+
+
+def idctn(x, type=2, s=None, axes=None, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, False, True)
+
+
+def dst(x, type=2, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, True, False)
+
+
+def idst(x, type=2, n=None, axis=-1, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    s, axes = _one_axis(n, axis)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, False, False)
+
+
+def dstn(x, type=2, s=None, axes=None, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, True, False)
+
+
+def idstn(x, type=2, s=None, axes=None, norm=None, overwrite_x=False, workers=None, orthogonalize=None):
+    _check_workers(workers)
+    return _r2rn(x, s, axes, type, norm, overwrite_x, orthogonalize, False, False)
+
+
+# ---------------------------------------------------------------------------------------------
+# helpers (rocket_fft/overloads.py:1214-1310, 1861-1871)
+# ---------------------------------------------------------------------------------------------
+
+def fftfreq(n, d=1.0, *, device=None):
+    """Sample frequencies [0, 1, ..., -(n//2)] / (n d): a NumPy array, or a float64 torch tensor
+    on `device` when one is given."""
+    n = int(n)
+    if n < 1:
+        raise ValueError("n must be positive")
+    k = np.empty(n, dtype=np.int64)
+    N = (n - 1) // 2 + 1
+    k[:N] = np.arange(N)
+    k[N:] = np.arange(-(n // 2), 0)
+    f = k * (1.0 / (n * d))
+    return f if device is None else _torch.as_tensor(f, device=device)
+
+
+def rfftfreq(n, d=1.0, *, device=None):
+    """Sample frequencies [0, 1, ..., n//2] / (n d) of a real transform."""
+    n = int(n)
+    if n < 1:
+        raise ValueError("n must be positive")
+    f = np.arange(n // 2 + 1) * (1.0 / (n * d))
+    return f if device is None else _torch.as_tensor(f, device=device)
+
+
+def _shift(x, axes, sign):
+    x = _asarray(x)
+    if axes is None:
+        axes = list(range(x.ndim))
+    else:
+        axes = [_wrap_axis(a, x.ndim) for a in np.atleast_1d(np.asarray(axes, dtype=np.int64))]
+    shifts = [0] * x.ndim
+    for ax in axes:
+        shifts[ax] += sign * (x.shape[ax] // 2)
+    out = _empty(x, x.shape, x.dtype)
+    _pf.roll(x, out, shifts)
+    return out
+
+
+def fftshift(x, axes=None):
+    """Shift the zero-frequency term to the centre (np.roll by n//2 along each axis)."""
+    return _shift(x, axes, 1)
+
+
+def ifftshift(x, axes=None):
+    """Inverse of fftshift (np.roll by -(n//2) along each axis)."""
+    return _shift(x, axes, -1)
+
+
+def next_fast_len(target, real=False):
+    """Smallest 11-smooth (real: 5-smooth) length >= target (pocketfft's good_size)."""
+    target = int(target)
+    if target < 0:
+        raise ValueError("Target cannot be negative.")
+    return _pf.good_size(target, bool(real))

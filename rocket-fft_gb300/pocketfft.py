@@ -324,6 +324,24 @@ def dct_adjoint(ain, aout, axes, type, fct, ortho, nthreads):
     _real_call("rocketgpu_dct_adjoint_st", ain, aout, axes, type, fct, ortho, nthreads)
 
 
+def roll(ain, aout, shifts):
+    """aout = ain cyclically shifted by shifts[d] along every dimension d (numpy.roll over all
+    axes); the index map of fftshift / ifftshift. Same shape and dtype, distinct arrays."""
+    a = _Arg(ain, "ain")
+    b = _Arg(aout, "aout")
+    if a.ndim != b.ndim:
+        raise TypingError("Input and output array must have the same number of dimensions")
+    sh = np.ascontiguousarray(np.asarray(shifts, dtype=np.int64).reshape(-1))
+    if sh.size != a.ndim:
+        raise ValueError("roll: one shift per dimension is required")
+    lib = _lib.load()
+    stream = a.stream or b.stream
+    lib.rocketgpu_set_stream(ctypes.c_void_p(stream) if stream is not None else None)
+    code = lib.rocketgpu_roll(a.ndim, ctypes.byref(a.struct), ctypes.byref(b.struct),
+                              sh.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    _raise_status(code, "rocketgpu_roll")
+
+
 def good_size(n, real):
     """Smallest fast length >= n: 2,3,5,7,11-smooth (``real=False``) or 2,3,5-smooth
     (``real=True``); ``rocket_fft/_pocketfft_numba.cpp:25-29``."""

@@ -1,0 +1,54 @@
+"""SciPy/NumPy-level front end (rocket-fft_gb300/fft.py, numpy_fft.py): argument handling that
+needs no GPU -- norm/axes/shape/type/workers validation as the reference's front end
+(rocket_fft/overloads.py:380-551, 680-732), next_fast_len bit-exact against scipy.fft, and the
+frequency helpers exact against numpy.fft."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import scipy.fft as sfft
+
+
+@pytest.fixture(scope="module")
+def F(rg):
+    return rg.fft
+
+
+def test_norm_and_axes_validation(F, rg):
+    x = np.ones((4, 6))
+    with pytest.raises(ValueError, match="norm"):
+        F.fft(x, norm="bad")
+    with pytest.raises(ValueError, match="unique"):
+        F.fftn(x, axes=(0, 0))
+    with pytest.raises(ValueError, match="same length"):
+        F.fftn(x, s=(4,), axes=(0, 1))
+    with pytest.raises(ValueError, match="data points"):
+        F.fft(x, n=0)
+    with pytest.raises(ValueError, match="more axes"):
+        F.fftn(x, s=(2, 2, 2))
+    with pytest.raises(ValueError, match="type"):
+        F.dct(x, type=5)
+    with pytest.raises(ValueError, match="Workers"):
+        F.fft(x, workers=0)
+    with pytest.raises(np.exceptions.AxisError if hasattr(np, "exceptions") else ValueError):
+        F.fft(x, axis=2)
+    with pytest.raises(TypeError):
+        F.rfft(x.astype(np.complex128))
+    with pytest.raises(ValueError, match="negative"):
+        F.next_fast_len(-1)
+
+
+def test_next_fast_len_matches_scipy(F):
+    for real in (False, True):
+        got = [F.next_fast_len(n, real) for n in range(1, 3000)]
+        want = [sfft.next_fast_len(n, real) for n in range(1, 3000)]
+        assert got == want
+
+
+def test_frequency_helpers(F, rg):
+    for n in (1, 2, 7, 8, 33):
+        for d in (1.0, 0.25):
+            assert np.array_equal(F.fftfreq(n, d), np.fft.fftfreq(n, d))
+            assert np.array_equal(F.rfftfreq(n, d), np.fft.rfftfreq(n, d))
+            assert np.array_equal(rg.numpy_fft.fftfreq(n, d), np.fft.fftfreq(n, d))

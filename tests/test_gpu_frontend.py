@@ -1,0 +1,183 @@
+"""SciPy/NumPy-level front end on the GPU: every transform of rocket-fft_gb300/fft.py and
+numpy_fft.py against scipy.fft / numpy.fft on the host, on CUDA tensors (and, for a subset, on
+NumPy arrays staged by the library). Tolerance: relative L2 <= 1e-6 (single precision),
+<= 1e-13 (double precision), as the rest of the suite; the reference's own comparison tests
+(tests/test_scipy_compare.py, test_numpy_compare.py) use rtol 1e-12 in double precision.
+
+One convention differs between the reference and current SciPy: for DST types II and III with
+orthonormalisation the reference's pocketfft scales element 0 (of the output for type II, of the
+input for type III; rocket_fft/_pocketfft_hdronly.h:3033-3041), SciPy 1.18 the last one. The
+front end follows the reference, so those cases are checked against the oracle."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import scipy.fft as sfft
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOLS = {np.float32: 1e-6, np.complex64: 1e-6, np.float64: 1e-13, np.complex128: 1e-13}
+
+
+def _rand(shape, dtype, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(shape)
+    if np.dtype(dtype).kind == "c":
+        x = x + 1j * rng.standard_normal(shape)
+    return x.astype(dtype)
+
+
+def _cmp(got, want, dtype):
+    g = got.cpu().numpy() if hasattr(got, "cpu") else np.asarray(got)
+    assert g.shape == want.shape, (g.shape, want.shape)
+    err = oracle.rel_l2(g, want)
+    single = np.dtype(dtype) in (np.dtype(np.float32), np.dtype(np.complex64))
+    assert err <= (1e-6 if single else 1e-13), err
+
+
+CASES = [
+    # name, kwargs, input shape
+    ("fft", dict(), (6, 40)),
+    ("fft", dict(n=50, axis=0, norm="ortho"), (33, 5)),
+    ("ifft", dict(n=24, norm="forward"), (3, 30)),
+    ("fft2", dict(s=(8, 20), norm="backward"), (6, 16)),
+    ("ifft2", dict(axes=(0, 2)), (6, 3, 10)),
+    ("fftn", dict(), (4, 6, 10)),
+    ("ifftn", dict(s=(5, 7), axes=(2, 0), norm="ortho"), (4, 6, 10)),
+    ("rfft", dict(n=64), (3, 50)),
+    ("irfft", dict(), (3, 33)),
+    ("irfft", dict(n=63, norm="ortho"), (3, 33)),
+    ("rfft2", dict(norm="forward"), (10, 12)),
+    ("irfft2", dict(s=(9, 14)), (10, 12)),
+    ("rfftn", dict(axes=(0, 2)), (8, 3, 12)),
+    ("irfftn", dict(), (8, 3, 7)),
+    ("hfft", dict(n=40), (2, 25)),
+    ("ihfft", dict(norm="ortho"), (2, 25)),
+    ("hfft2", dict(), (6, 9)),
+    ("ihfft2", dict(), (6, 9)),
+    ("hfftn", dict(s=(4, 5, 12)), (4, 5, 6)),
+    ("ihfftn", dict(axes=(1, 2)), (4, 5, 6)),
+]
+
+
+def _in_dtype(name, dtype):
+    real_only = name in ("rfft", "rfft2", "rfftn", "ihfft", "ihfft2", "ihfftn")
+    if real_only:
+        return np.float32 if dtype in (np.float32, np.complex64) else np.float64
+    return dtype
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128, np.float64])
+@pytest.mark.parametrize("name,kw,shape", CASES)
+def test_scipy_transforms(rg, cuda, name, kw, shape, dtype):
+    torch = cuda
+    dt = _in_dtype(name, dtype)
+    x = _rand(shape, dt, 1)
+    want = getattr(sfft, name)(x, **kw)
+    got = getattr(rg.fft, name)(torch.from_numpy(x).cuda(), **kw)
+    assert got.is_cuda
+    _cmp(got, want, dt)
+
+
+@pytest.mark.parametrize("cosine", [True, False])
+@pytest.mark.parametrize("type_", [1, 2, 3, 4])
+@pytest.mark.parametrize("norm", [None, "ortho", "forward"])
+def test_scipy_dct_dst(rg, cuda, cosine, type_, norm):
+    torch = cuda
+    x = _rand((5, 24), np.float64, 2)
+    name = "dct" if cosine else "dst"
+    for fn, kw in ((name, dict(type=type_, norm=norm)), ("i" + name, dict(type=type_, norm=norm)),
+                   (name + "n", dict(type=type_, norm=norm, s=(7, 20))),
+                   ("i" + name + "n", dict(type=type_, norm=norm, axes=(0,)))):
+        got = getattr(rg.fft, fn)(torch.from_numpy(x).cuda(), **kw)
+        if not cosine and type_ in (2, 3) and norm == "ortho":
+            want = _oracle_dst_ortho(x, fn, kw)
+        else:
+            want = getattr(sfft, fn)(x, **kw)
+        _cmp(got, want, np.float64)
+    # orthogonalize given explicitly, single precision, complex input (parts transformed apart)
+    x32 = _rand((4, 32), np.float32, 3)
+    _cmp(getattr(rg.fft, name)(torch.from_numpy(x32).cuda(), type=type_, norm="ortho", orthogonalize=False),
+         getattr(sfft, name)(x32, type=type_, norm="ortho", orthogonalize=False), np.float32)
+    if not (not cosine and type_ in (2, 3) and norm == "ortho"):
+        xc = _rand((3, 16), np.complex128, 4)
+        _cmp(getattr(rg.fft, name)(torch.from_numpy(xc).cuda(), type=type_, norm=norm),
+             getattr(sfft, name)(xc, type=type_, norm=norm), np.complex128)
+
+
+def _oracle_dst_ortho(x, fn, kw):
+    """The reference's orthonormal DST-II/III (oracle port), with the front end's shape, axes,
+    type swap and scaling: fct = 1/sqrt(prod 2 n) over the axes."""
+    inverse = fn.startswith("i")
+    t = {2: 3, 3: 2}[kw["type"]] if inverse else kw["type"]
+    if fn.endswith("n"):
+        axes = list(kw.get("axes", range(x.ndim))) if "s" not in kw else list(range(x.ndim - len(kw["s"]), x.ndim))
+        s = kw.get("s")
+    else:
+        axes, s = [x.ndim - 1], None
+    xin = x
+    if s is not None:
+        shape = list(x.shape)
+        for n, ax in zip(s, axes):
+            shape[ax] = n
+        xin = np.zeros(shape)
+        sl = tuple(slice(0, min(a, b)) for a, b in zip(x.shape, shape))
+        xin[sl] = x[sl]
+    fct = 1.0 / np.sqrt(np.prod([2.0 * xin.shape[a] for a in axes]))
+    out = np.empty_like(xin)
+    oracle.port().dst(np.ascontiguousarray(xin), out, axes, t, fct, True)
+    return out
+
+
+def test_overwrite_x(rg, cuda):
+    torch = cuda
+    x = _rand((4, 32), np.complex128, 5)
+    xd = torch.from_numpy(x).cuda()
+    out = rg.fft.fft(xd, overwrite_x=True)
+    assert out.data_ptr() == xd.data_ptr()
+    _cmp(out, sfft.fft(x), np.complex128)
+    y = _rand((4, 32), np.complex128, 6)
+    yd = torch.from_numpy(y).cuda()
+    out = rg.fft.fft(yd)
+    assert out.data_ptr() != yd.data_ptr()
+    _cmp(yd, y, np.complex128)  # input untouched
+
+
+def test_numpy_namespace(rg, cuda):
+    torch = cuda
+    x = _rand((6, 10), np.complex128, 7)
+    xd = torch.from_numpy(x).cuda()
+    _cmp(rg.numpy_fft.fftn(xd, axes=(1, 1)), np.fft.fftn(x, axes=(1, 1)), np.complex128)  # repeated axis
+    out = torch.empty_like(xd)
+    res = rg.numpy_fft.ifft2(xd, out=out)
+    assert res is out
+    _cmp(out, np.fft.ifft2(x), np.complex128)
+    r = _rand((5, 18), np.float64, 8)
+    _cmp(rg.numpy_fft.rfft(torch.from_numpy(r).cuda(), n=20), np.fft.rfft(r, n=20), np.float64)
+    _cmp(rg.numpy_fft.hfft(torch.from_numpy(x).cuda()), np.fft.hfft(x), np.float64)
+
+
+def test_host_arrays(rg, cuda):
+    """NumPy inputs run through the same kernels (staged by the library) and return NumPy."""
+    x = _rand((8, 30), np.float32, 9)
+    got = rg.fft.rfftn(x, norm="ortho")
+    assert isinstance(got, np.ndarray)
+    _cmp(got, sfft.rfftn(x, norm="ortho"), np.float32)
+    z = _rand((6, 12), np.complex128, 10)
+    _cmp(rg.fft.ifft(z, n=16), sfft.ifft(z, n=16), np.complex128)
+    _cmp(rg.fft.dctn(z.real.copy(), type=1), sfft.dctn(z.real, type=1), np.float64)
+
+
+@pytest.mark.parametrize("axes", [None, 0, (1,), (0, 2)])
+def test_fftshift(rg, cuda, axes):
+    torch = cuda
+    for dt in (np.float32, np.complex128, np.int64):
+        x = (np.arange(5 * 6 * 7).reshape(5, 6, 7) * 1.5).astype(dt)
+        xd = torch.from_numpy(x).cuda()
+        assert np.array_equal(rg.fft.fftshift(xd, axes).cpu().numpy(), np.fft.fftshift(x, axes))
+        assert np.array_equal(rg.fft.ifftshift(xd, axes).cpu().numpy(), np.fft.ifftshift(x, axes))
+    x = np.arange(9.0)
+    assert np.array_equal(rg.numpy_fft.fftshift(x), np.fft.fftshift(x))
