@@ -13,6 +13,8 @@ the reference's low-level signatures, host arrays only):
   ``rocket_fft/_pocketfft_hdronly.h`` compiled in place by ``make -C oracle ref``; only exists
   where the reference tree exists (not on the GPU host). Also offers ``long double``
   transforms (``ld_*``) as the higher-precision answer.
+
+``oracle.fftlog`` restates the reference's FFTLog (fast Hankel transform) on ``port()``.
 """
 
 from __future__ import annotations

@@ -41,6 +41,7 @@ __all__ = [
     "fft", "ifft", "fft2", "ifft2", "fftn", "ifftn", "rfft", "irfft", "rfft2", "irfft2", "rfftn",
     "irfftn", "hfft", "ihfft", "hfft2", "ihfft2", "hfftn", "ihfftn", "dct", "idct", "dctn", "idctn",
     "dst", "idst", "dstn", "idstn", "fftfreq", "rfftfreq", "fftshift", "ifftshift", "next_fast_len",
+    "fht", "ifht", "fhtoffset",
 ]
 
 
@@ -496,3 +497,128 @@ def next_fast_len(target, real=False):
     if target < 0:
         raise ValueError("Target cannot be negative.")
     return _pf.good_size(target, bool(real))
+
+
+# ---------------------------------------------------------------------------------------------
+# FFTLog: fast Hankel transform (rocket_fft/overloads.py:857-902, 1755-1806, 1844-1857)
+# ---------------------------------------------------------------------------------------------
+#
+# Hamilton's FFTLog (MNRAS 312, 2000) for a sequence a_j sampled at log-spaced points
+# r_j = r_c exp((j - j_c) dln), j_c = (n - 1)/2: with a power-law bias q applied as
+# exp(-q (j - j_c) dln), the transform is rfft -> multiply by the coefficients u_m -> irfft ->
+# reverse, where
+#     u_m = 2^q Gamma(x+ + i y_m) / Gamma(x- - i y_m) exp(2 i y_m (ln 2 - ln kr)),
+#     x+- = (mu + 1 +- q) / 2,  y_m = pi m / (n dln),  m = 0 .. n//2,
+# the last coefficient made real (for every n, as the reference does; SciPy 1.18 does so only
+# for even n), and a pole at m = 0 replaced by its limit 2^q Gamma(x+) / Gamma(x-) (the
+# Pochhammer symbol (x-)_{x+ - x-}). The inverse divides by conj(u_m). The n//2 + 1
+# coefficients are computed in double on the host (log-gamma of complex arguments); both FFTs
+# run in the library's kernels. As in the reference, dln, mu, offset and bias are first
+# rounded to the array's real precision.
+
+def _fht_scalar(x, pos, name):
+    import numbers
+
+    if isinstance(x, (bool, np.bool_)) or not isinstance(x, numbers.Real):
+        raise TypeError(f"The {pos} argument '{name}' must be a real scalar.")
+    return float(x)
+
+
+def _fht_args(x, args, names, first):
+    x = _asarray(x)
+    if _kind(x) == "c":
+        raise TypeError(f"The 1st argument '{first}' must be a real array.")
+    x = _cast(x, _dtype(x, False))
+    rnd = np.float32 if _single(x) else np.float64
+    vals = [float(rnd(_fht_scalar(v, pos, nm))) for v, pos, nm in zip(args, ("2nd", "3rd", "4th", "5th"), names)]
+    return x, vals
+
+
+def _fht_coeff(n, dln, mu, offset, bias):
+    from scipy import special
+
+    q = bias
+    xp = (mu + 1 + q) / 2
+    xm = (mu + 1 - q) / 2
+    y = np.linspace(0, np.pi * (n // 2) / (n * dln), n // 2 + 1)
+    lp = special.loggamma(xp + 1j * y)
+    lm = special.loggamma(xm + 1j * y)
+    u = np.exp((lp.real - lm.real + np.log(2) * q) + 1j * (lp.imag + lm.imag + 2 * y * (np.log(2) - offset)))
+    u[-1] = u[-1].real
+    if not np.isfinite(u[0]):
+        u[0] = 2**q * special.poch(xm, xp - xm)
+    return u
+
+
+def _like(w, x, dtype=None):
+    """Host float64/complex128 vector `w` as an array of x's kind (device, precision)."""
+    if _is_torch(x):
+        return _torch.as_tensor(w, device=x.device).to(dtype or x.dtype)
+    return w.astype(dtype or x.dtype)
+
+
+def _flip_last(x):
+    return _torch.flip(x, dims=(-1,)) if _is_torch(x) else np.ascontiguousarray(x[..., ::-1])
+
+
+def _fht_run(x, u, inverse):
+    import warnings
+
+    n = x.shape[-1]
+    if inverse:
+        if u[0] == 0:
+            warnings.warn("singular inverse transform; consider changing the bias", stacklevel=3)
+            u[0] = np.inf
+        X = rfft(x)
+        X = X / _like(np.conj(u), X)
+    else:
+        if np.isinf(u[0]):
+            warnings.warn("singular transform; consider changing the bias", stacklevel=3)
+            u[0] = 0
+        X = rfft(x)
+        X = X * _like(u, X)
+    return _flip_last(irfft(X, n))
+
+
+def fht(a, dln, mu, offset=0.0, bias=0.0):
+    """Fast Hankel transform along the last axis (scipy.fft.fht)."""
+    a, (dln, mu, offset, bias) = _fht_args(a, (dln, mu, offset, bias), ("dln", "mu", "offset", "bias"), "a")
+    n = a.shape[-1]
+    jd = (np.arange(n) - (n - 1) / 2) * dln
+    if bias != 0:
+        a = a * _like(np.exp(-bias * jd), a)
+    A = _fht_run(a, _fht_coeff(n, dln, mu, offset, bias), False)
+    if bias != 0:
+        A = A * _like(np.exp(-bias * (jd + offset)), A)
+    return A
+
+
+def ifht(A, dln, mu, offset=0.0, bias=0.0):
+    """Inverse fast Hankel transform along the last axis (scipy.fft.ifht)."""
+    A, (dln, mu, offset, bias) = _fht_args(A, (dln, mu, offset, bias), ("dln", "mu", "offset", "bias"), "A")
+    n = A.shape[-1]
+    jd = (np.arange(n) - (n - 1) / 2) * dln
+    if bias != 0:
+        A = A * _like(np.exp(bias * (jd + offset)), A)
+    a = _fht_run(A, _fht_coeff(n, dln, mu, offset, bias), True)
+    if bias != 0:
+        a = a / _like(np.exp(-bias * jd), a)
+    return a
+
+
+def fhtoffset(dln, mu, initial=0.0, bias=0.0):
+    """Optimal offset ln(kr) for the fast Hankel transform (scipy.fft.fhtoffset,
+    overloads.py:1844-1857): the offset nearest `initial` that makes the last coefficient real."""
+    from scipy import special
+
+    dln = _fht_scalar(dln, "1st", "dln")
+    mu = _fht_scalar(mu, "2nd", "mu")
+    initial = _fht_scalar(initial, "3rd", "initial")
+    q = _fht_scalar(bias, "4th", "bias")
+    xp = (mu + 1 + q) / 2
+    xm = (mu + 1 - q) / 2
+    y = np.pi / (2 * dln)
+    zp = special.loggamma(xp + 1j * y)
+    zm = special.loggamma(xm + 1j * y)
+    arg = (np.log(2) - initial) / dln + (zp.imag + zm.imag) / np.pi
+    return initial + (arg - np.round(arg)) * dln

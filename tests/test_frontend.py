@@ -52,3 +52,53 @@ def test_frequency_helpers(F, rg):
             assert np.array_equal(F.fftfreq(n, d), np.fft.fftfreq(n, d))
             assert np.array_equal(F.rfftfreq(n, d), np.fft.rfftfreq(n, d))
             assert np.array_equal(rg.numpy_fft.fftfreq(n, d), np.fft.fftfreq(n, d))
+
+
+@pytest.mark.parametrize("n", [8, 16, 32, 64])
+@pytest.mark.parametrize("dln", [0.05, 0.1])
+@pytest.mark.parametrize("mu", [0.0, 0.5, 1.5])
+@pytest.mark.parametrize("offset", [0.0, 0.3])
+@pytest.mark.parametrize("bias", [0.0, 0.7])
+def test_fftlog_oracle_pinned(n, dln, mu, offset, bias):
+    """The FFTLog oracle against scipy.fft.fht / ifht on the reference's own grid of cases
+    (even n, where the two coefficient conventions coincide): relative L2 <= 1e-14."""
+    import oracle
+    from oracle import fftlog
+
+    a = np.random.default_rng(12).standard_normal(n)
+    A = fftlog.fht(a, dln, mu, offset, bias)
+    assert oracle.rel_l2(A, sfft.fht(a, dln, mu, offset=offset, bias=bias)) <= 1e-14
+    assert oracle.rel_l2(fftlog.ifht(A, dln, mu, offset, bias), sfft.ifht(A, dln, mu, offset=offset, bias=bias)) <= 1e-14
+
+
+@pytest.mark.parametrize("dln", [0.05, 0.1, 0.2])
+@pytest.mark.parametrize("mu", [0.0, 0.5, 1.0, 2.5])
+@pytest.mark.parametrize("initial", [0.0, 0.3])
+@pytest.mark.parametrize("bias", [0.0, 0.8])
+def test_fhtoffset_matches_scipy(F, dln, mu, initial, bias):
+    assert F.fhtoffset(dln, mu, initial=initial, bias=bias) == sfft.fhtoffset(dln, mu, initial=initial, bias=bias)
+
+
+def test_fftlog_argument_validation(F):
+    x = np.random.default_rng(0).random(7)
+    for fn in (F.fht, F.ifht):
+        with pytest.raises(TypeError, match="real array"):
+            fn(x.astype(np.complex128), 1.0, 1.0)
+        for bad in ([1.0], "1.0", True):
+            with pytest.raises(TypeError, match="dln"):
+                fn(x, bad, 1.0)
+            with pytest.raises(TypeError, match="mu"):
+                fn(x, 1.0, bad)
+            with pytest.raises(TypeError, match="offset"):
+                fn(x, 1.0, 1.0, bad)
+            with pytest.raises(TypeError, match="bias"):
+                fn(x, 1.0, 1.0, 1.0, bad)
+    for bad in ([1.0], "1.0", True):
+        with pytest.raises(TypeError, match="dln"):
+            F.fhtoffset(bad, 1.0)
+        with pytest.raises(TypeError, match="mu"):
+            F.fhtoffset(1.0, bad)
+        with pytest.raises(TypeError, match="initial"):
+            F.fhtoffset(1.0, 1.0, bad)
+        with pytest.raises(TypeError, match="bias"):
+            F.fhtoffset(1.0, 1.0, 1.0, bad)

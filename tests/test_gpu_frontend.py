@@ -181,3 +181,61 @@ def test_fftshift(rg, cuda, axes):
         assert np.array_equal(rg.fft.ifftshift(xd, axes).cpu().numpy(), np.fft.ifftshift(x, axes))
     x = np.arange(9.0)
     assert np.array_equal(rg.numpy_fft.fftshift(x), np.fft.fftshift(x))
+
+
+
+
+def _fht_tol(n, dln, bias):
+    """1e-13 times the half-span exp(|bias| n dln / 2) of the bias weights, which scale the two
+    ends of the sequence apart before the FFT and back after it (two correct float64 FFTs
+    differ by that much)."""
+    return 1e-13 * np.exp(abs(bias) * n * dln / 2)
+
+
+@pytest.mark.parametrize("mu,offset,bias", [(0.0, 0.0, 0.0), (0.5, 0.3, 0.0), (1.5, 0.0, 0.7), (-0.5, 0.25, -0.4)])
+@pytest.mark.parametrize("n", [8, 64, 101, 4096])
+def test_fht(rg, cuda, mu, offset, bias, n):
+    """FFTLog (scipy.fft.fht / ifht) against the FFTLog oracle for every n and against SciPy for
+    even n (SciPy makes the last coefficient real only then; the reference always does).
+    float64: relative L2 <= _fht_tol; float32: <= 1e-6 of the float64 answer at the
+    float32-rounded parameters."""
+    torch = cuda
+    from oracle import fftlog
+
+    dln = 0.05 if n < 1000 else 0.0005
+    tol = _fht_tol(n, dln, bias)
+    rng = np.random.default_rng(12)
+    a = rng.standard_normal((3, n))
+    want = fftlog.fht(a, dln, mu, offset, bias)
+    got = rg.fft.fht(torch.from_numpy(a).cuda(), dln, mu, offset=offset, bias=bias)
+    assert got.dtype == torch.float64 and got.is_cuda
+    assert oracle.rel_l2(got.cpu().numpy(), want) <= tol
+    if n % 2 == 0:
+        assert oracle.rel_l2(got.cpu().numpy(), sfft.fht(a, dln, mu, offset=offset, bias=bias)) <= tol
+    # the inverse on the same input as the oracle's
+    back = rg.fft.ifht(torch.from_numpy(want).cuda(), dln, mu, offset=offset, bias=bias)
+    assert oracle.rel_l2(back.cpu().numpy(), fftlog.ifht(want, dln, mu, offset, bias)) <= tol
+    f32 = lambda v: float(np.float32(v))
+    want32 = fftlog.fht(a.astype(np.float32), f32(dln), f32(mu), f32(offset), f32(bias))
+    got32 = rg.fft.fht(a.astype(np.float32), dln, mu, offset=offset, bias=bias)
+    assert got32.dtype == np.float32
+    assert oracle.rel_l2(got32, want32) <= 1e-6
+
+
+@pytest.mark.parametrize("n", [64, 101])
+def test_fht_singular(rg, cuda, n):
+    """A pole of Gamma(x+) at m = 0 (mu = -1.5, bias = 0.5) zeroes the forward coefficient, a pole
+    of Gamma(x-) (mu = 1, bias = 2) makes the inverse singular: both warn, as the reference
+    does, and still match the oracle."""
+    torch = cuda
+    from oracle import fftlog
+
+    dln = 0.05
+    a = np.random.default_rng(5).standard_normal((3, n))
+    with pytest.warns(UserWarning, match="singular transform"):
+        got = rg.fft.fht(torch.from_numpy(a).cuda(), dln, -1.5, bias=0.5)
+    assert oracle.rel_l2(got.cpu().numpy(), fftlog.fht(a, dln, -1.5, 0.0, 0.5)) <= _fht_tol(n, dln, 0.5)
+    A = fftlog.fht(a, dln, 1.0, 0.0, 2.0)
+    with pytest.warns(UserWarning, match="singular inverse"):
+        back = rg.fft.ifht(torch.from_numpy(A).cuda(), dln, 1.0, bias=2.0)
+    assert oracle.rel_l2(back.cpu().numpy(), fftlog.ifht(A, dln, 1.0, 0.0, 2.0)) <= _fht_tol(n, dln, 2.0)
