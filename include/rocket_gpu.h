@@ -239,6 +239,14 @@ int rocketgpu_c2c_noalloc(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocke
  * 256 x 32, B, B2 32 x 32 float16 (row-major, device), D 256 x 32 float32 (device). */
 int rocketgpu_set_tc_split(int on);
 int rocketgpu_tc_error(void *stream);
+
+/* Two-axis plane kernels (no reference counterpart; off unless switched on here or by
+ * ROCKET_GPU_PLANE=1). While on, an r2c over two or more axes whose last axis (contiguous, even
+ * power-of-two length) and the axis before it fit one of the compiled plane sizes runs those
+ * two axes in one pass, one thread-block cluster per plane with the transposition through
+ * distributed shared memory; c2r likewise. Measured slower than the axis-by-axis kernels on
+ * GB300, kept as a tested alternative. Returns the previous setting. */
+int rocketgpu_set_plane_kernels(int on);
 int rocketgpu_tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D, void *stream);
 
 /* N-d cyclic shift, numpy.roll semantics over every dimension: out[(i_d + shifts[d]) mod n_d] =

@@ -32,6 +32,7 @@ from .pocketfft import (  # noqa: F401
     roll,
     set_stream,
     set_tc_split,
+    set_plane_kernels,
     tc_error,
     tc_selftest,
     version,

@@ -92,6 +92,8 @@ def _declare(lib):
     lib.rocketgpu_roll.restype = i32
     lib.rocketgpu_set_tc_split.argtypes = [i32]
     lib.rocketgpu_set_tc_split.restype = i32
+    lib.rocketgpu_set_plane_kernels.argtypes = [i32]
+    lib.rocketgpu_set_plane_kernels.restype = i32
     lib.rocketgpu_tc_error.argtypes = [P]
     lib.rocketgpu_tc_error.restype = i32
     lib.rocketgpu_tc_selftest.argtypes = [P, P, P, P, P, P]

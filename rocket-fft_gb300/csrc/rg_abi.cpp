@@ -494,6 +494,8 @@ RG_EXPORT uint64_t rocketgpu_launch_count(void) { return rg::launch_count(); }
 
 RG_EXPORT int rocketgpu_set_tc_split(int on) { return rg::set_tc_split(on != 0); }
 
+RG_EXPORT int rocketgpu_set_plane_kernels(int on) { return rg::set_plane_kernels(on != 0); }
+
 RG_EXPORT int rocketgpu_roll(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t *aout,
                              const int64_t *shifts) {
   return guarded([&] {

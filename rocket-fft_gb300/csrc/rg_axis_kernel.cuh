@@ -14,6 +14,7 @@
 // general_r2c / general_c2r (rocket_fft/_pocketfft_hdronly.h:3568-3607, 3723-3852): rows
 // processed as SIMD lanes there are processed as CTA rows here.
 #pragma once
+#include "rg_pdl.cuh"
 #include "rg_fft.cuh"
 
 namespace rg {
@@ -69,6 +70,7 @@ __device__ __forceinline__ cx<T> load_unit(const void *base, int64_t off, int i,
 template <typename T, int OP>
 __global__ void __launch_bounds__(512) axis_kernel(const __grid_constant__ KArgs a, FastDiv dTB,
                                                    FastDiv dIn, FastDiv dOut) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char smraw[];
   const int TB = a.TB;
   const int pitch = a.pitch, ps = a.ps;

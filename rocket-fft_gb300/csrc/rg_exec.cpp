@@ -13,6 +13,7 @@
 #include "rg_exec.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -20,6 +21,7 @@
 #include "rg_error.hpp"
 #include "rg_exec_detail.hpp"
 #include "rg_launch.hpp"
+#include "rg_plane.hpp"
 
 namespace rg {
 
@@ -221,6 +223,20 @@ bool fixed_enabled() {
     return !(e && e[0] == '0');
   }();
   return on;
+}
+
+// The plane kernels (rg_plane.cuh) are off unless ROCKET_GPU_PLANE=1 or set_plane_kernels(true):
+// on GB300 they measured slower than the axis-by-axis kernels.
+static std::atomic<int> g_plane{-1};
+bool plane_enabled() {
+  int v = g_plane.load(std::memory_order_relaxed);
+  if (v < 0) {
+    const char *e = std::getenv("ROCKET_GPU_PLANE");
+    int want = (e && e[0] == '1') ? 1 : 0;
+    g_plane.compare_exchange_strong(v, want);
+    v = g_plane.load(std::memory_order_relaxed);
+  }
+  return v != 0;
 }
 
 // Reciprocals of the batch extents for 32-bit row decomposition; false if an extent does not
@@ -626,6 +642,102 @@ void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
             nullptr, st);
 }
 
+// ---------------------------------------------------------------------------------------
+// two-axis plane jobs (rg_plane.cuh): the last axis (real, contiguous) and the axis before it
+// in the axis list, one cluster per plane
+// ---------------------------------------------------------------------------------------
+
+int log2_exact(int64_t n) {
+  if (n < 1 || (n & (n - 1))) return -1;
+  int e = 0;
+  while ((int64_t(1) << e) < n) ++e;
+  return e;
+}
+
+struct PlaneGeo {
+  int a1 = -1, last = -1, E1 = 0, E2 = 0;
+  int64_t L1 = 0, n2 = 0, H = 0, nplanes = 0;
+  Batch b;  // the dimensions other than a1 and last (strides: complex side, real side)
+};
+
+// Plane geometry of an r2c (real = in, cplx = out) or c2r (cplx = in, real = out) request,
+// false when no plane kernel applies: the real side must hold contiguous, aligned pairs along
+// the last axis, the complex side unit stride along it.
+bool plane_geo(DType dt, const NdArray &real, const NdArray &cplx, const Axes &axes, PlaneGeo &g) {
+  if (axes.size() < 2 || !plane_enabled() || !fixed_enabled() || !pow2_enabled() || stream_enabled() ||
+      tc_split_enabled())
+    return false;
+  g.last = int(axes.back());
+  g.a1 = int(axes[axes.size() - 2]);
+  if (g.a1 == g.last) return false;
+  g.n2 = real.shape[g.last];
+  g.L1 = real.shape[g.a1];
+  g.E1 = int(log2_exact(g.L1));
+  g.E2 = int(log2_exact(g.n2));
+  if (g.E1 < 0 || g.E2 < 0 || plane_cluster(dt, g.E1, g.E2) == 0) return false;
+  g.H = g.n2 / 2;
+  if (real.stride[g.last] != 1 || cplx.stride[g.last] != 1) return false;
+  if (reinterpret_cast<uintptr_t>(real.data) % (2 * real_size(dt)) != 0 || real.stride[g.a1] % 2 != 0) return false;
+  std::vector<int64_t> shape = real.shape;
+  shape[g.a1] = 1;
+  g.b = make_batch(shape, cplx.stride, real.stride, g.last);
+  for (int64_t sr : g.b.s_out)
+    if (sr % 2 != 0) return false;
+  if (g.b.shape.size() + 1 > size_t(kMaxBatchDims)) return false;
+  g.nplanes = g.b.nrows;
+  return g.nplanes * g.L1 < (int64_t(1) << 31) && g.nplanes * g.H < (int64_t(1) << 31);
+}
+
+// r2c along `last` then c2c along `a1`, in -> out, fct applied once. True if it ran.
+bool plane_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, double fct, cudaStream_t st) {
+  PlaneGeo g;
+  if (!plane_geo(dt, in, out, axes, g)) return false;
+  KArgs ar{}, ac{};
+  ar.in = in.data;
+  ar.ld = with_inner(make_side(1, g.b.shape, g.b.s_out), g.L1, in.stride[g.a1], 1);
+  ar.nrows = g.L1 * g.nplanes;
+  ar.core = get_core(int(g.H), dt).core;
+  ar.aux = get_roots(uint64_t(g.n2), uint64_t(g.H / 2 + 1), dt);
+  ar.fct = 1.0;
+  ac.out = out.data;
+  ac.st = with_inner(make_side(out.stride[g.a1], g.b.shape, g.b.s_in), g.H, out.stride[g.last], out.stride[g.a1]);
+  ac.nrows = g.H * g.nplanes;
+  ac.core = get_core(int(g.L1), dt).core;
+  ac.fct = fct;
+  if (!set_fastdivs(ar.ld) || !set_fastdivs(ac.st)) return false;
+  const uint64_t bytes = uint64_t(g.nplanes * g.L1) * (uint64_t(g.n2) * real_size(dt) + uint64_t(g.H + 1) * cx_size(dt));
+  bool ran = false;
+  profiled_launch(dt == DType::F32 ? "plane_r2c_f32" : "plane_r2c_f64", bytes, st,
+                  [&] { ran = launch_plane(dt, false, g.E1, g.E2, ar, ac, g.nplanes, st); });
+  RG_CHECK(ran, RG_ERR_INTERNAL, "plane kernel instance missing");
+  return true;
+}
+
+// c2c backward along `a1` then c2r along `last`, src -> out with fct. True if it ran.
+bool plane_c2r(DType dt, const NdArray &src, const NdArray &out, const Axes &axes, double fct, cudaStream_t st) {
+  PlaneGeo g;
+  if (!plane_geo(dt, out, src, axes, g)) return false;
+  KArgs ar{}, ac{};
+  ac.in = src.data;
+  ac.ld = with_inner(make_side(src.stride[g.a1], g.b.shape, g.b.s_in), g.H, src.stride[g.last], src.stride[g.a1]);
+  ac.nrows = g.H * g.nplanes;
+  ac.core = get_core(int(g.L1), dt).core;
+  ac.fct = 1.0;
+  ar.out = out.data;
+  ar.st = with_inner(make_side(1, g.b.shape, g.b.s_out), g.L1, out.stride[g.a1], 1);
+  ar.nrows = g.L1 * g.nplanes;
+  ar.core = get_core(int(g.H), dt).core;
+  ar.aux = get_roots(uint64_t(g.n2), uint64_t(g.H / 2 + 1), dt);
+  ar.fct = fct;
+  if (!set_fastdivs(ac.ld) || !set_fastdivs(ar.st)) return false;
+  const uint64_t bytes = uint64_t(g.nplanes * g.L1) * (uint64_t(g.n2) * real_size(dt) + uint64_t(g.H + 1) * cx_size(dt));
+  bool ran = false;
+  profiled_launch(dt == DType::F32 ? "plane_c2r_f32" : "plane_c2r_f64", bytes, st,
+                  [&] { ran = launch_plane(dt, true, g.E1, g.E2, ar, ac, g.nplanes, st); });
+  RG_CHECK(ran, RG_ERR_INTERNAL, "plane kernel instance missing");
+  return true;
+}
+
 bool any_zero(const std::vector<int64_t> &shape) {
   for (int64_t s : shape)
     if (s == 0) return true;
@@ -635,6 +747,12 @@ bool any_zero(const std::vector<int64_t> &shape) {
 }  // namespace detail
 
 using namespace detail;
+
+int set_plane_kernels(bool on) {
+  const int prev = plane_enabled() ? 1 : 0;
+  g_plane.store(on ? 1 : 0, std::memory_order_relaxed);
+  return prev;
+}
 
 // ---------------------------------------------------------------------------------------
 // public driver
@@ -658,6 +776,16 @@ void exec_r2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
               double fct, cudaStream_t st, double bscale) {
   if (any_zero(in.shape) || axes.empty()) return;
   const int last = int(axes.back());
+  if (forward && bscale == 1.0 && plane_r2c(dt, in, out, axes, fct, st)) {
+    // the last two axes in one pass; the rest in place
+    if (axes.size() > 2) {
+      NdArray o = out;
+      o.shape = in.shape;
+      o.shape[last] = in.shape[last] / 2 + 1;
+      exec_c2c(dt, o, o, Axes(axes.begin(), axes.end() - 2), forward, 1.0, st);
+    }
+    return;
+  }
   const Batch b = make_batch(in.shape, in.stride, out.stride, last);
   const Side ld = make_side(in.stride[last], b.shape, b.s_in);
   const Side sd = make_side(out.stride[last], b.shape, b.s_out);
@@ -682,6 +810,26 @@ void exec_c2r(DType dt, const NdArray &in, const NdArray &out, const Axes &axes,
     const Side sd = make_side(out.stride[last], b.shape, b.s_out);
     c2r_rows(dt, out.shape[last], in.data, ld, out.data, sd, b.nrows, forward, fct, st, bscale);
     return;
+  }
+  if (!forward && bscale == 1.0) {
+    // the last two axes in one pass (after the other axes, into a temporary, if any)
+    NdArray src = in;
+    src.shape = shape_in;
+    if (axes.size() == 2 && plane_c2r(dt, src, out, axes, fct, st)) return;
+    NdArray t;  // C-contiguous temporary for the other axes
+    t.shape = shape_in;
+    t.stride.assign(shape_in.size(), 1);
+    for (int d = int(shape_in.size()) - 2; d >= 0; --d) t.stride[d] = t.stride[d + 1] * shape_in[d + 1];
+    PlaneGeo g;
+    if (axes.size() > 2 && plane_geo(dt, out, t, axes, g)) {
+      int64_t total = 1;
+      for (int64_t s : shape_in) total *= s;
+      DevBuf tmp(size_t(total) * cx_size(dt), st);
+      t.data = tmp.get();
+      exec_c2c(dt, src, t, Axes(axes.begin(), axes.end() - 2), forward, 1.0, st);
+      RG_CHECK(plane_c2r(dt, t, out, axes, fct, st), RG_ERR_INTERNAL, "plane geometry changed");
+      return;
+    }
   }
   // C-contiguous complex temporary with the input's shape
   int64_t total = 1;

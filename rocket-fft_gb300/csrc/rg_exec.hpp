@@ -20,6 +20,9 @@ struct NdArray {
 
 using Axes = std::vector<uint64_t>;
 
+// Two-axis plane kernels on or off (process-wide); returns the previous setting.
+int set_plane_kernels(bool on);
+
 void exec_c2c(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool forward,
               double fct, cudaStream_t st);
 // bscale: extra scale of the interior half-spectrum bins along the last axis (0 < k < n/2):

@@ -23,6 +23,7 @@
 //             reordering / pre-twiddle, passes, post-twiddle / un-reordering on the last store
 #pragma once
 #include "rg_axis_kernel.cuh"
+#include "rg_pdl.cuh"
 
 namespace rg {
 namespace fx {
@@ -121,11 +122,10 @@ template <int TB, int LR, bool COL> __device__ __forceinline__ void fx_rj(int bf
 
 // Inputs of butterfly (r, j) of pass p: gathered from global memory (pass 0) or shared memory,
 // twiddled and transformed in registers.
-template <typename T, int OP, int E, int P, bool COL, bool BWD, int SRC>
+template <typename T, int OP, int E, int P, bool COL, bool BWD, int SRC, typename C = FxCfg<T, OP, E, COL>>
 __device__ __forceinline__ void fx_compute(const KArgs &a, uint32_t row0, int r, int j, const cx<T> *__restrict__ src,
                                            const cx<T> *__restrict__ tw, bool pair_ok,
                                            cx<T> (&v)[fx::radix_of(E, P)]) {
-  using C = FxCfg<T, OP, E, COL>;
   constexpr int L = C::L, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P), TWO = fx::tw_of(E, P);
   constexpr int PS = C::PS, PITCH = C::PITCH;
   if constexpr (SRC == FX_GLOBAL) {
@@ -167,10 +167,9 @@ __device__ __forceinline__ void fx_compute(const KArgs &a, uint32_t row0, int r,
 
 // Outputs of butterfly (r, j) of pass p: to shared memory, or (last pass of C2C / C2R_EVEN)
 // to global memory with the op's output conversion.
-template <typename T, int OP, int E, int P, bool COL, bool BWD, int DST>
+template <typename T, int OP, int E, int P, bool COL, bool BWD, int DST, typename C = FxCfg<T, OP, E, COL>>
 __device__ __forceinline__ void fx_emit(const KArgs &a, uint32_t row0, int r, int j, cx<T> *__restrict__ dst,
                                         bool scale, bool pair_ok, const cx<T> (&v)[fx::radix_of(E, P)]) {
-  using C = FxCfg<T, OP, E, COL>;
   constexpr int R = fx::radix_of(E, P), NS = fx::ns_of(E, P);
   constexpr int PS = C::PS, PITCH = C::PITCH;
   const int m = j & (NS - 1);
@@ -272,11 +271,12 @@ __device__ __forceinline__ void fx_emit(const KArgs &a, uint32_t row0, int r, in
 
 // One radix pass p of the compile-time schedule. Rows r >= rows (tail tile) are skipped.
 // INPL: source and destination are the same shared buffer; every butterfly of the CTA reads
-// its inputs (and transforms them) before a barrier, then all write.
-template <typename T, int OP, int E, int P, bool COL, bool BWD, int SRC, int DST, bool INPL = false>
+// its inputs (and transforms them) before a barrier, then all write. C: the geometry (rows per
+// CTA, threads, shared pitch); FxCfg for the axis kernels, the plane kernels bring their own.
+template <typename T, int OP, int E, int P, bool COL, bool BWD, int SRC, int DST, bool INPL = false,
+          typename C = FxCfg<T, OP, E, COL>>
 __device__ __forceinline__ void fx_pass(const KArgs &a, uint32_t row0, int rows, const cx<T> *src, cx<T> *dst,
                                         const cx<T> *__restrict__ tw, bool scale, bool pair_ok) {
-  using C = FxCfg<T, OP, E, COL>;
   constexpr int L = C::L, R = fx::radix_of(E, P), LR = L / R;
   constexpr int TB = C::TB, NT = C::NT;
   constexpr int NBF = TB * LR;
@@ -290,8 +290,8 @@ __device__ __forceinline__ void fx_pass(const KArgs &a, uint32_t row0, int rows,
       fx_rj<TB, LR, COL>(bf, r, j);
       if (r >= rows) continue;
       cx<T> v[R];
-      fx_compute<T, OP, E, P, COL, BWD, SRC>(a, row0, r, j, src, tw, pair_ok, v);
-      fx_emit<T, OP, E, P, COL, BWD, DST>(a, row0, r, j, dst, scale, pair_ok, v);
+      fx_compute<T, OP, E, P, COL, BWD, SRC, C>(a, row0, r, j, src, tw, pair_ok, v);
+      fx_emit<T, OP, E, P, COL, BWD, DST, C>(a, row0, r, j, dst, scale, pair_ok, v);
     }
   } else {
     static_assert(SRC == FX_SMEM && DST == FX_SMEM, "in-place passes stay on chip");
@@ -301,7 +301,7 @@ __device__ __forceinline__ void fx_pass(const KArgs &a, uint32_t row0, int rows,
       const int bf = int(threadIdx.x) + it * NT;
       int r, j;
       fx_rj<TB, LR, COL>(bf, r, j);
-      if ((NBF % NT == 0 || bf < NBF) && r < rows) fx_compute<T, OP, E, P, COL, BWD, SRC>(a, row0, r, j, src, tw, pair_ok, v[it]);
+      if ((NBF % NT == 0 || bf < NBF) && r < rows) fx_compute<T, OP, E, P, COL, BWD, SRC, C>(a, row0, r, j, src, tw, pair_ok, v[it]);
     }
     __syncthreads();
 #pragma unroll
@@ -309,17 +309,82 @@ __device__ __forceinline__ void fx_pass(const KArgs &a, uint32_t row0, int rows,
       const int bf = int(threadIdx.x) + it * NT;
       int r, j;
       fx_rj<TB, LR, COL>(bf, r, j);
-      if ((NBF % NT == 0 || bf < NBF) && r < rows) fx_emit<T, OP, E, P, COL, BWD, DST>(a, row0, r, j, dst, scale, pair_ok, v[it]);
+      if ((NBF % NT == 0 || bf < NBF) && r < rows) fx_emit<T, OP, E, P, COL, BWD, DST, C>(a, row0, r, j, dst, scale, pair_ok, v[it]);
+    }
+  }
+}
+
+// The split of one unit of the last R2C_EVEN pass: v1, v2 are the DFT outputs of the
+// butterflies j1 = u and j2 = NS - u (u = 0: j1 = 0, j2 = NS / 2), whose outputs Z_{j + q NS}
+// hold both members of every pair (k, L - k); put(k, X_k) receives every bin 0 <= k <= L once.
+//     X_k = E + W_2L^k O,  X_{L-k} = conj(E - W_2L^k O),  E = (Z_k + conj Z_{L-k}) / 2,
+//     O = -i (Z_k - conj Z_{L-k}) / 2,   X_0 = Re Z_0 + Im Z_0,  X_L = Re Z_0 - Im Z_0.
+template <typename T, int L, int R, int NS, typename Put>
+__device__ __forceinline__ void fx_split_unit(int u, const cx<T> (&v1)[R], const cx<T> (&v2)[R],
+                                              const cx<T> *__restrict__ w, Put &&put) {
+  const int j2 = u == 0 ? NS / 2 : NS - u;
+  // Slot q of a unit: the pair (ka, L - ka), ka <= L / 2, from za = Z_ka, zb = Z_{L-ka}:
+  //   u >= 1, q < R/2:   (u + q NS, v1[q], v2[R-1-q]);  q >= R/2: (j2 + (R-1-q) NS, v2[R-1-q], v1[q])
+  //   u = 0:   q = 0: (0, v1[0], v1[0]) -- the split formula then gives X_0 and X_L;
+  //            1 <= q < R/2: (q NS, v1[q], v1[R-q]);  q = R/2: (L/2, v1[R/2], v1[R/2]), one output;
+  //            R/2 < q <= R: (NS/2 + (q-R/2-1) NS, v2[q-R/2-1], v2[R-1-(q-R/2-1)])
+  // All lanes run the same R + 1 slots (the last only for u = 0); operands are selected, not
+  // branched on, so the unit-0 lanes of a warp do not diverge.
+  const bool u0 = u == 0;
+#pragma unroll
+  for (int q = 0; q <= R; ++q) {
+    // general unit
+    int kg = 0;
+    cx<T> zag = v1[0], zbg = v1[0];
+    if (q < R / 2) {
+      kg = u + q * NS;
+      zag = v1[q];
+      zbg = v2[R - 1 - q];
+    } else if (q < R) {
+      kg = j2 + (R - 1 - q) * NS;
+      zag = v2[R - 1 - q];
+      zbg = v1[q];
+    }
+    // unit 0
+    int k0;
+    cx<T> za0, zb0;
+    bool two0 = true;
+    if (q == 0) {
+      k0 = 0;
+      za0 = v1[0];
+      zb0 = v1[0];
+    } else if (q < R / 2) {
+      k0 = q * NS;
+      za0 = v1[q];
+      zb0 = v1[R - q];
+    } else if (q == R / 2) {
+      k0 = L / 2;
+      za0 = v1[R / 2];
+      zb0 = v1[R / 2];
+      two0 = false;
+    } else {
+      const int qq = q - R / 2 - 1;
+      k0 = NS / 2 + qq * NS;
+      za0 = v2[qq];
+      zb0 = v2[R - 1 - qq];
+    }
+    const int ka = u0 ? k0 : kg;
+    const cx<T> za = u0 ? za0 : zag, zb = u0 ? zb0 : zbg;
+    const bool two = u0 ? two0 : true;
+    if (u0 || q < R) {
+      const cx<T> zc = cj<T>(zb);
+      const cx<T> Ev = scl<T>(add<T>(za, zc), T(0.5));
+      const cx<T> O = mnegi<T>(scl<T>(sub<T>(za, zc), T(0.5)));
+      const cx<T> t = mul<T>(__ldg(w + ka), O);
+      put(ka, add<T>(Ev, t));
+      if (two) put(L - ka, cj<T>(sub<T>(Ev, t)));
     }
   }
 }
 
 // Last pass of R2C_EVEN with the split fused in (last radix <= 8). Unit (r, u) transforms the
-// butterflies j1 = u and j2 = NS - u (u = 0: j1 = 0, j2 = NS / 2) of row r, whose outputs
-// Z_{j + q NS} hold both members of every pair (k, L - k); it splits them in registers,
-//     X_k = E + W_2L^k O,  X_{L-k} = conj(E - W_2L^k O),  E = (Z_k + conj Z_{L-k}) / 2,
-//     O = -i (Z_k - conj Z_{L-k}) / 2,   X_0 = Re Z_0 + Im Z_0,  X_L = Re Z_0 - Im Z_0,
-// and stores X straight to global memory.
+// butterflies j1 = u and j2 = NS - u of row r (fx_split_unit) and stores X straight to global
+// memory.
 template <typename T, int E, bool COL>
 __device__ __forceinline__ void fx_r2c_last_split(const KArgs &a, uint32_t row0, int rows, const cx<T> *buf,
                                                   const cx<T> *__restrict__ tw) {
@@ -368,88 +433,32 @@ __device__ __forceinline__ void fx_r2c_last_split(const KArgs &a, uint32_t row0,
       dft<T, R>(v2);
     }
     cx<T> *p = reinterpret_cast<cx<T> *>(a.out) + side_offset32(a.st, row0 + uint32_t(r));
-    auto put = [&](int i, cx<T> x) {
+    fx_split_unit<T, L, R, NS>(u, v1, v2, w, [&](int i, cx<T> x) {
       if (!plain) {
         if (i != 0 && i != L) x = scl<T>(x, bsc);
         x = mk<T>(x.x * fct, (cout ? -x.y : x.y) * fct);
       }
       p[i * s] = x;
-    };
-    // Slot q of a unit: the pair (ka, L - ka), ka <= L / 2, from za = Z_ka, zb = Z_{L-ka}:
-    //   u >= 1, q < R/2:   (u + q NS, v1[q], v2[R-1-q]);  q >= R/2: (j2 + (R-1-q) NS, v2[R-1-q], v1[q])
-    //   u = 0:   q = 0: (0, v1[0], v1[0]) -- the split formula then gives X_0 and X_L;
-    //            1 <= q < R/2: (q NS, v1[q], v1[R-q]);  q = R/2: (L/2, v1[R/2], v1[R/2]), one output;
-    //            R/2 < q <= R: (NS/2 + (q-R/2-1) NS, v2[q-R/2-1], v2[R-1-(q-R/2-1)])
-    // All lanes run the same R + 1 slots (the last only for u = 0); operands are selected, not
-    // branched on, so the unit-0 lanes of a warp do not diverge.
-    const bool u0 = u == 0;
-#pragma unroll
-    for (int q = 0; q <= R; ++q) {
-      // general unit
-      int kg = 0;
-      cx<T> zag = v1[0], zbg = v1[0];
-      if (q < R / 2) {
-        kg = u + q * NS;
-        zag = v1[q];
-        zbg = v2[R - 1 - q];
-      } else if (q < R) {
-        kg = j2 + (R - 1 - q) * NS;
-        zag = v2[R - 1 - q];
-        zbg = v1[q];
-      }
-      // unit 0
-      int k0;
-      cx<T> za0, zb0;
-      bool two0 = true;
-      if (q == 0) {
-        k0 = 0;
-        za0 = v1[0];
-        zb0 = v1[0];
-      } else if (q < R / 2) {
-        k0 = q * NS;
-        za0 = v1[q];
-        zb0 = v1[R - q];
-      } else if (q == R / 2) {
-        k0 = L / 2;
-        za0 = v1[R / 2];
-        zb0 = v1[R / 2];
-        two0 = false;
-      } else {
-        const int qq = q - R / 2 - 1;
-        k0 = NS / 2 + qq * NS;
-        za0 = v2[qq];
-        zb0 = v2[R - 1 - qq];
-      }
-      const int ka = u0 ? k0 : kg;
-      const cx<T> za = u0 ? za0 : zag, zb = u0 ? zb0 : zbg;
-      const bool two = u0 ? two0 : true;
-      if (u0 || q < R) {
-        const cx<T> zc = cj<T>(zb);
-        const cx<T> Ev = scl<T>(add<T>(za, zc), T(0.5));
-        const cx<T> O = mnegi<T>(scl<T>(sub<T>(za, zc), T(0.5)));
-        const cx<T> t = mul<T>(__ldg(w + ka), O);
-        put(ka, add<T>(Ev, t));
-        if (two) put(L - ka, cj<T>(sub<T>(Ev, t)));
-      }
-    }
+    });
   }
 }
 
 // Passes 1 .. NP-2 in place in buffer A (the first reads global memory or A, the last writes
 // global memory or stays in A).
-template <typename T, int OP, int E, bool COL, bool BWD, int P, int PEND>
+template <typename T, int OP, int E, bool COL, bool BWD, int P, int PEND, typename C = FxCfg<T, OP, E, COL>>
 __device__ __forceinline__ void fx_middle(const KArgs &a, uint32_t row0, int rows, cx<T> *buf, const cx<T> *tw,
                                           bool scale, bool pair_ok) {
   if constexpr (P < PEND) {
-    fx_pass<T, OP, E, P, COL, BWD, FX_SMEM, FX_SMEM, true>(a, row0, rows, buf, buf, tw, scale, pair_ok);
+    fx_pass<T, OP, E, P, COL, BWD, FX_SMEM, FX_SMEM, true, C>(a, row0, rows, buf, buf, tw, scale, pair_ok);
     __syncthreads();
-    fx_middle<T, OP, E, COL, BWD, P + 1, PEND>(a, row0, rows, buf, tw, scale, pair_ok);
+    fx_middle<T, OP, E, COL, BWD, P + 1, PEND, C>(a, row0, rows, buf, tw, scale, pair_ok);
   }
 }
 
 template <typename T, int OP, int E, bool COL, bool BWD>
 __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
     fixed_kernel(const __grid_constant__ KArgs a, int pair_ok_i) {
+  pdl_begin();
   using C = FxCfg<T, OP, E, COL>;
   constexpr int L = C::L, NP = C::NP, TB = C::TB, NT = C::NT, PS = C::PS, PITCH = C::PITCH;
   constexpr int TPR = NT / TB;  // threads per row in the staged loops

@@ -15,7 +15,7 @@ void fx_launch(const KArgs &a, int pair_ok, cudaStream_t st) {
   set_smem_attr(fn, C::SMEM);
   const int64_t grid = (a.nrows + C::TB - 1) / C::TB;
   RG_CHECK(grid < (int64_t(1) << 31), RG_ERR_UNSUPPORTED, "too many transforms in one call");
-  fixed_kernel<T, OP, E, COL, BWD><<<unsigned(grid), C::NT, C::SMEM, st>>>(a, pair_ok);
+  launch_pdl(&fixed_kernel<T, OP, E, COL, BWD>, dim3(unsigned(grid)), dim3(C::NT), C::SMEM, st, a, pair_ok);
 }
 
 template <typename T, int OP, bool COL, bool BWD>

@@ -2,6 +2,7 @@
 #include "rg_launch.hpp"
 
 #include <atomic>
+#include <cstdlib>
 #include <functional>
 #include <cstring>
 #include <map>
@@ -24,6 +25,15 @@ void launch_mirror_f64(const MirrorArgs &a, cudaStream_t st);
 
 static std::atomic<uint64_t> g_launches{0};
 static std::atomic<int> g_tc{0};
+
+// Programmatic dependent launch of the chained kernels (rg_pdl.cuh); ROCKET_GPU_PDL=0 turns it off.
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("ROCKET_GPU_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 bool tc_split_enabled() { return g_tc.load(std::memory_order_relaxed) != 0; }
 int set_tc_split(bool on) { return g_tc.exchange(on ? 1 : 0); }

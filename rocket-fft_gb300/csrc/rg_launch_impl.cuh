@@ -9,6 +9,7 @@
 #include "rg_stream_kernel.cuh"
 #include "rg_error.hpp"
 #include "rg_launch.hpp"
+#include "rg_pdl.cuh"
 
 namespace rg {
 
@@ -50,7 +51,7 @@ void launch_axis_t(const KArgs &a, const LaunchCfg &cfg, cudaStream_t st) {
     if (cfg.pow2) {
       const void *fn = reinterpret_cast<const void *>(&pow2_kernel<T, OP>);
       ensure_smem_attr(fn, cfg.smem);
-      pow2_kernel<T, OP><<<cfg.grid, cfg.threads, cfg.smem, st>>>(a, dTB, dIn, dOut);
+      launch_pdl(&pow2_kernel<T, OP>, dim3(cfg.grid), dim3(cfg.threads), cfg.smem, st, a, dTB, dIn, dOut);
       note_launch();
       RG_CUDA(cudaGetLastError());
       return;
@@ -58,7 +59,7 @@ void launch_axis_t(const KArgs &a, const LaunchCfg &cfg, cudaStream_t st) {
   }
   const void *fn = reinterpret_cast<const void *>(&axis_kernel<T, OP>);
   ensure_smem_attr(fn, cfg.smem);
-  axis_kernel<T, OP><<<cfg.grid, cfg.threads, cfg.smem, st>>>(a, dTB, dIn, dOut);
+  launch_pdl(&axis_kernel<T, OP>, dim3(cfg.grid), dim3(cfg.threads), cfg.smem, st, a, dTB, dIn, dOut);
   note_launch();
   RG_CUDA(cudaGetLastError());
 }
@@ -84,6 +85,7 @@ template <typename T> void launch_axis_typed(int op, const KArgs &a, const Launc
 
 template <typename T, int OP>
 __global__ void __launch_bounds__(256) pointwise_kernel(const __grid_constant__ PwArgs a) {
+  pdl_begin();
   const int n = a.n;
   const T fct = T(a.fct);
   for (int64_t g = blockIdx.y; g < a.nrows; g += gridDim.y) {
@@ -149,7 +151,7 @@ template <typename T, int OP> void launch_pw_t(const PwArgs &a, cudaStream_t st)
   const int64_t target = 16384 / int64_t(gx) + 1;  // enough CTAs to fill the GPU
   if (gy > target) gy = target;
   if (gy > 65535) gy = 65535;
-  pointwise_kernel<T, OP><<<dim3(gx, unsigned(gy)), threads, 0, st>>>(a);
+  launch_pdl(&pointwise_kernel<T, OP>, dim3(gx, unsigned(gy)), dim3(threads), 0, st, a);
   note_launch();
   RG_CUDA(cudaGetLastError());
 }
@@ -172,6 +174,7 @@ template <typename T> void launch_pw_typed(int op, const PwArgs &a, cudaStream_t
 // ---------------------------------------------------------------------------------------
 
 template <typename T> __global__ void __launch_bounds__(256) mirror_kernel(const __grid_constant__ MirrorArgs a) {
+  pdl_begin();
   cx<T> *d = reinterpret_cast<cx<T> *>(a.data);
   for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < a.total;
        idx += int64_t(gridDim.x) * blockDim.x) {
@@ -201,7 +204,7 @@ template <typename T> void launch_mirror_typed(const MirrorArgs &a, cudaStream_t
   if (a.total <= 0) return;
   int64_t blocks = (a.total + 255) / 256;
   if (blocks > 152 * 32) blocks = 152 * 32;
-  mirror_kernel<T><<<unsigned(blocks), 256, 0, st>>>(a);
+  launch_pdl(&mirror_kernel<T>, dim3(unsigned(blocks)), dim3(256), 0, st, a);
   note_launch();
   RG_CUDA(cudaGetLastError());
 }

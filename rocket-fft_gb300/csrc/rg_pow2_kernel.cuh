@@ -123,6 +123,7 @@ template <typename T, int OP>
 __global__ void __launch_bounds__(512) pow2_kernel(const __grid_constant__ KArgs a, FastDiv dTB, FastDiv dIn,
                                                    FastDiv dOut) {
   static_assert(OP == OP_C2C || OP == OP_C2C_TW || OP == OP_R2C_EVEN || OP == OP_C2R_EVEN, "op");
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char smraw[];
   P2 c;
   c.TB = a.TB;

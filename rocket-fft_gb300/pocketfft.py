@@ -23,7 +23,9 @@ integers; violations raise :class:`TypingError`. ``nthreads`` is accepted and ig
 from __future__ import annotations
 
 import ctypes
+import math
 import numbers
+import struct
 
 import numpy as np
 
@@ -121,6 +123,41 @@ def _axes_array(axes):
 
 _CAI_ITEMSIZE = {"<f4": 4, "<f8": 8, "<c8": 8, "<c16": 16}
 
+# numba array struct (numba/_arraystruct.h): meminfo, parent, nitems, itemsize, data, then
+# ndim extents and ndim byte strides, all 8-byte fields; packed in one call per argument.
+_PACKERS: dict[int, tuple] = {}
+
+
+def _packer(ndim):
+    p = _PACKERS.get(ndim)
+    if p is None:
+        p = (struct.Struct("<QQqqQ" + "q" * max(2 * ndim, 1)), _lib.struct_type(ndim))
+        _PACKERS[ndim] = p
+    return p
+
+
+def _struct(ndim, nitems, itemsize, ptr, shape, strides):
+    S, T = _packer(ndim)
+    if ndim:
+        return T.from_buffer_copy(S.pack(0, 0, nitems, itemsize, ptr, *shape, *strides))
+    return T.from_buffer_copy(S.pack(0, 0, nitems, itemsize, ptr, 0))
+
+
+if _torch is not None:
+    _TORCH_KIND = {_torch.float32: (4, "f"), _torch.float64: (8, "f"), _torch.complex64: (8, "c"),
+                   _torch.complex128: (16, "c"), _torch.float16: (2, "f"), _torch.bfloat16: (2, "f")}
+    # the raw current-stream accessor (a few hundred ns) when this torch has it, else the public call
+    _raw_stream = getattr(_torch._C, "_cuda_getCurrentRawStream", None)
+else:  # pragma: no cover
+    _TORCH_KIND = {}
+    _raw_stream = None
+
+
+def _torch_stream(t):
+    if _raw_stream is not None:
+        return _raw_stream(t.get_device())
+    return _torch.cuda.current_stream(t.device).cuda_stream
+
 
 class _Arg:
     """An array argument turned into a numba array struct (kept alive with its owner)."""
@@ -133,11 +170,15 @@ class _Arg:
         if isinstance(a, np.ndarray):
             self._from_parts(a.ctypes.data, a.shape, a.strides, a.itemsize, a.dtype.kind, False)
         elif _torch is not None and isinstance(a, _torch.Tensor):
-            es = a.element_size()
-            kind = "c" if a.is_complex() else ("f" if a.is_floating_point() else "i")
-            self._from_parts(a.data_ptr(), tuple(a.shape), tuple(s * es for s in a.stride()), es, kind, a.is_cuda)
-            if a.is_cuda:
-                self.stream = _torch.cuda.current_stream(a.device).cuda_stream
+            k = _TORCH_KIND.get(a.dtype)
+            if k is None:
+                es = a.element_size()
+                k = (es, "c" if a.is_complex() else ("f" if a.is_floating_point() else "i"))
+            es, kind = k
+            cuda = a.is_cuda
+            self._from_parts(a.data_ptr(), a.shape, [s * es for s in a.stride()], es, kind, cuda)
+            if cuda:
+                self.stream = _torch_stream(a)
         elif hasattr(a, "__cuda_array_interface__"):
             cai = a.__cuda_array_interface__
             typestr = cai["typestr"]
@@ -160,16 +201,7 @@ class _Arg:
 
     def _from_parts(self, ptr, shape, strides, itemsize, kind, cuda):
         ndim = len(shape)
-        st = _lib.struct_type(ndim)()
-        st.meminfo = None
-        st.parent = None
-        st.nitems = int(np.prod(shape)) if ndim else 1
-        st.itemsize = itemsize
-        st.data = ptr
-        for i in range(ndim):
-            st.shape_and_strides[i] = int(shape[i])
-            st.shape_and_strides[ndim + i] = int(strides[i])
-        self.struct = st
+        self.struct = _struct(ndim, math.prod(shape), itemsize, ptr, shape, strides)
         self.ndim = ndim
         self.itemsize = itemsize
         self.kind = kind
@@ -177,13 +209,26 @@ class _Arg:
 
 
 def _axes_struct(ax):
-    st = _lib.struct_type(1)()
-    st.nitems = ax.size
-    st.itemsize = 8
-    st.data = ax.ctypes.data
-    st.shape_and_strides[0] = ax.size
-    st.shape_and_strides[1] = 8
-    return st
+    return _struct(1, ax.size, 8, ax.ctypes.data, (ax.size,), (8,))
+
+
+# validated axes (uint64 copy + descriptor) by the caller's array contents
+_AXES_CACHE: dict = {}
+
+
+def _axes_prepared(axes):
+    if isinstance(axes, np.ndarray) and axes.ndim == 1:
+        key = (axes.dtype.str, axes.tobytes())
+        hit = _AXES_CACHE.get(key)
+        if hit is not None:
+            return hit
+        ax = _axes_array(axes)
+        if len(_AXES_CACHE) > 256:
+            _AXES_CACHE.clear()
+        hit = _AXES_CACHE[key] = (ax, _axes_struct(ax))
+        return hit
+    ax = _axes_array(axes)
+    return ax, _axes_struct(ax)
 
 
 def _raise_status(code, fname):
@@ -204,21 +249,22 @@ def _prepare(ain, aout, axes):
     b = _Arg(aout, "aout")
     if a.ndim != b.ndim:
         raise TypingError("Input and output array must have the same number of dimensions")
-    ax = _axes_array(axes)
-    return a, b, ax
+    return a, b, _axes_prepared(axes)
+
+
+_FNS: dict = {}
 
 
 def _call(fname, a, b, ax, *rest):
-    lib = _lib.load()
+    fn = _FNS.get(fname)
+    if fn is None:
+        lib = _lib.load()
+        fn = _FNS[fname] = (getattr(lib, fname), lib.rocketgpu_set_stream)
     stream = a.stream or b.stream
-    if stream is not None:
-        lib.rocketgpu_set_stream(ctypes.c_void_p(stream))
-    else:
-        lib.rocketgpu_set_stream(None)
-    axs = _axes_struct(ax)
-    fn = getattr(lib, fname)
-    code = fn(a.ndim, ctypes.byref(a.struct), ctypes.byref(b.struct), ctypes.byref(axs), *rest)
-    _raise_status(code, fname[:-3])
+    fn[1](stream)
+    code = fn[0](a.ndim, ctypes.byref(a.struct), ctypes.byref(b.struct), ctypes.byref(ax[1]), *rest)
+    if code:
+        _raise_status(code, fname[:-3])
 
 
 # ---------------------------------------------------------------------------------------
@@ -372,6 +418,15 @@ def set_tc_split(on=True):
     stages on the tensor cores (FP16 hi/lo operands, FP32 accumulation); everything else
     keeps the plain kernels. No counterpart in rocket-fft."""
     return bool(_lib.load().rocketgpu_set_tc_split(1 if on else 0))
+
+
+def set_plane_kernels(on=True):
+    """Switch the two-axis plane kernels on or off (process-wide); returns the previous
+    setting. While on, r2c / c2r over two or more axes run the last axis and the one before it
+    in one pass, one thread-block cluster per plane (distributed shared memory for the
+    transposition). Off by default: slower than the axis-by-axis kernels on GB300. No
+    counterpart in rocket-fft."""
+    return bool(_lib.load().rocketgpu_set_plane_kernels(1 if on else 0))
 
 
 def tc_error(stream=None):
