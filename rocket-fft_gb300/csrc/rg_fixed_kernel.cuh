@@ -55,6 +55,18 @@ __host__ __device__ constexpr int pitch_of(int lsm, int ps, int esz) {
   while (p % (128 / esz) != 1) ++p;
   return p;
 }
+// Column walk: lanes run across the TB rows first, then along the positions. A warp's shared
+// access is served one 128-byte line of lanes at a time (16 complex64 or 8 complex128 lanes),
+// which covers TB rows x line / TB positions when TB < line: lane (r, j) lands on slot
+// pitch * r + j of the line, so the pitch must be line / TB modulo the line for the slots to be
+// distinct (1 when TB >= line).
+__host__ __device__ constexpr int pitch_col(int lsm, int ps, int esz, int TB) {
+  const int line = 128 / esz;
+  const int want = TB < line ? line / TB : 1;
+  int p = lsm + ((lsm - 1) >> ps) + 1;
+  while (p % line != want) ++p;
+  return p;
+}
 __host__ __device__ constexpr int clampi(int x, int lo, int hi) { return x < lo ? lo : x > hi ? hi : x; }
 // Row walk: when a bank line's worth of lanes spans several rows (g = L / 16 lanes per row in
 // the first pass and the staged loops, g < elements per bank line), rows start g slots apart
@@ -76,9 +88,9 @@ template <typename T, int OP, int E, bool COL> struct FxCfg {
   static constexpr int ESZ = int(2 * sizeof(T));
   static constexpr int PS = sizeof(T) == 4 ? 4 : 3;
   static constexpr int LSM = (OP == OP_C2C || OP == OP_DCT2 || OP == OP_DCT3) ? L : L + 1;
-  static constexpr int PITCH = COL ? fx::pitch_of(LSM, PS, ESZ) : fx::pitch_row(LSM, PS, ESZ, L);
   static constexpr int TB = COL ? (sizeof(T) == 4 ? (L <= 256 ? 16 : 8) : (L <= 256 ? 8 : 4))
                                 : ((sizeof(T) == 4 ? 4096 : 2048) / L > 1 ? (sizeof(T) == 4 ? 4096 : 2048) / L : 1);
+  static constexpr int PITCH = COL ? fx::pitch_col(LSM, PS, ESZ, TB) : fx::pitch_row(LSM, PS, ESZ, L);
   static constexpr int NT = fx::clampi(TB * L / 16, 64, 512);
   static constexpr int NBUF = OP == OP_C2C && NP == 1 ? 0 : 1;  // middle passes run in place
   static constexpr size_t SMEM = size_t(NBUF) * TB * PITCH * ESZ;

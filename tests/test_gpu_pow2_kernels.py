@@ -44,6 +44,10 @@ C2C_CASES = [
     ((2048, 512), (1,), np.complex128, True, 1.0),
     ((256, 2048), (0,), np.complex128, False, 0.5),
     ((64, 4096), (1, 0), np.complex64, True, 1.0),
+    # strided complex64 axes of 512 / 1024 points: 8 columns per CTA
+    ((1024, 96), (0,), np.complex64, True, 1.0),
+    ((16, 512, 40), (1,), np.complex64, False, 1.0 / 512),
+    ((8, 1024, 513), (1, 2), np.complex64, True, 1.0),
 ]
 
 
@@ -70,6 +74,8 @@ REAL_CASES = [
     ((8192, 256), (1,), np.float64, 1.0),
     ((256, 8192), (0,), np.float32, 2.0),      # strided real axis: scalar (unpaired) loads
     ((512, 128, 64), (2, 1), np.float64, 1.0),
+    ((2048, 48), (0,), np.float32, 1.0),       # strided real axes of 1024 / 512 complex points
+    ((1024, 3, 20), (0,), np.float32, 1.0),
 ]
 
 
@@ -123,6 +129,8 @@ DCT_CASES = [
     ((512, 300), (0,), np.float32, 3, False, True, 1.0),
     ((64, 64, 256), (0, 1, 2), np.float64, 2, True, True, 1.0),
     ((2048, 128), (1, 0), np.float64, 3, False, False, 2.0),
+    ((1024, 40), (0,), np.float32, 2, True, True, 1.0),
+    ((2048, 24), (0,), np.float32, 3, False, False, 1.0),
 ]
 
 
