@@ -205,6 +205,30 @@ void set_smem_attr(const void *fn, size_t smem) {
   done.emplace_back(fn, dev);
 }
 
+int64_t resident_ctas(const void *fn, int threads, size_t smem) {
+  struct Ent {
+    const void *fn;
+    int threads, dev;
+    size_t smem;
+    int64_t ctas;
+  };
+  static std::mutex mu;
+  static std::vector<Ent> cache;
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Ent &e : cache)
+      if (e.fn == fn && e.threads == threads && e.smem == smem && e.dev == dev) return e.ctas;
+  }
+  int per_sm = 0;
+  RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+  const int64_t ctas = int64_t(per_sm) * sm_count();
+  std::lock_guard<std::mutex> lk(mu);
+  cache.push_back({fn, threads, dev, smem, ctas});
+  return ctas;
+}
+
 int sm_count() {
   static int cache[64] = {};
   int dev = 0;
