@@ -150,6 +150,22 @@ def timed_steps(torch, step, steps, warmup, local, world):
     return ms, clk.summary(), rg.launch_count() - launches0
 
 
+def e2e_rate(torch, steps, h2d, run, d2h, units):
+    """End to end: every step copies its input from pinned host memory (`h2d`), runs the
+    library's public call (`run`) and copies its result back to pinned host memory (`d2h`), all
+    on the current stream; wall clock over `steps` steps after one untimed step, with a device
+    synchronisation at both ends. Returns units per second."""
+    h2d(); run(); d2h()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h2d()
+        run()
+        d2h()
+    torch.cuda.synchronize()
+    return units * steps / (time.perf_counter() - t0)
+
+
 def kernel_profile(step, steps):
     """Per-kernel device time and algorithmic bytes over `steps` steps (events around every
     launch of the library); returns (stats, roofline dict of the dominant kernel)."""
@@ -270,11 +286,28 @@ def run_c4(args):
     xg = xs[0].detach()[:1].clone().requires_grad_(True)
     (W[:1] * ops.rfftn(xg, axes)).abs().square().sum().backward()
     err = float((xg.grad.double().cpu() - x0.grad).norm() / x0.grad.norm())
+    # end to end: the input volume from pinned host memory, the gradient back to it
+    xh = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+    xh.copy_(xs[0].detach().cpu())
+    gh = torch.empty_like(xh, pin_memory=True)
+    xe = xs[0]
+
+    def e2e_in():
+        with torch.no_grad():
+            xe.copy_(xh, non_blocking=True)
+
+    def e2e_run():
+        xe.grad = None
+        (W * ops.rfftn(xe, axes)).abs().square().sum().backward()
+
+    e2e = {"value": e2e_rate(torch, args.steps, e2e_in, e2e_run, lambda: gh.copy_(xe.grad, non_blocking=True), 128),
+           "unit": "transforms/s", "h2d_bytes_per_step": xh.numel() * 4, "d2h_bytes_per_step": gh.numel() * 4,
+           "path": "torch_ops.rfftn forward + adjoint on a pinned host volume copied in, gradient copied out"}
     line = base_line(METRIC, value, "transforms/s", world, args, ms, "f32",
                      {"workload": "rfftn float32 64 x 1024 x 1024 axes (1,2), loss sum|W*X|^2, forward + adjoint",
                       "global_batch": 64 * world, "l2": "2 rotating 256 MiB inputs > L2"})
     line.update({"roofline": roof, "kernels": kernels, "accuracy": {"grad_rel_l2_vs_torch_fp64": err},
-                 "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clocks})
+                 "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -313,6 +346,19 @@ def run_c5(args):
     ms_plain = t0.elapsed_time(t1) / steps
     kernels, roof = kernel_profile(step, 1)
     diff = float(torch.linalg.vector_norm(state["u"] - u64) / torch.linalg.vector_norm(u64))
+    # end to end: the right-hand side from pinned host memory, the solution back to it
+    fh = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    fh.copy_(f.cpu())
+    uh = torch.empty_like(fh, pin_memory=True)
+    fe = torch.empty_like(f)
+
+    def e2e_run():
+        state["ue"], _ = S.solve(fe, mixed=True, tol=1e-12)
+
+    e2e = {"value": e2e_rate(torch, steps, lambda: fe.copy_(fh, non_blocking=True), e2e_run,
+                             lambda: uh.copy_(state["ue"], non_blocking=True), 1),
+           "unit": "solves/s", "h2d_bytes_per_step": fh.numel() * 8, "d2h_bytes_per_step": uh.numel() * 8,
+           "path": "poisson.NeumannPoisson.solve on a pinned host right-hand side copied in, solution copied out"}
     a = argparse.Namespace(steps=steps, warmup=min(args.warmup, 3))
     line = base_line("solves/s", world * steps / (ms / 1e3), "solves/s", world, a, ms, "f32 transforms + f64 refinement",
                      {"workload": "Neumann Poisson, 512^3 float64 RHS = 64 Gaussian blobs (zero mean), "
@@ -324,7 +370,7 @@ def run_c5(args):
                               "plain_rel_residual": info_plain["rel_residual"],
                               "mixed_vs_plain_rel_l2": diff},
                  "fp64_plain_form": {"ms_per_solve": ms_plain, "solves_per_s": 1e3 / ms_plain},
-                 "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clocks})
+                 "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -404,6 +450,14 @@ def run_c3(args):
     with ThreadPoolExecutor(cores) as ex:
         list(ex.map(cpu_rows, [sample[i::cores] for i in range(cores)]))
     cpu_s = time.perf_counter() - t0
+    # end to end: the batch from pinned host memory, the spectra back to it
+    bh = torch.empty(plan.total, dtype=torch.complex64, pin_memory=True)
+    bh.copy_(x.cpu())
+    oh = torch.empty_like(bh, pin_memory=True)
+    e2e = {"value": e2e_rate(torch, args.steps, lambda: x.copy_(bh, non_blocking=True), plan.replay,
+                             lambda: oh.copy_(y, non_blocking=True), len(lengths)),
+           "unit": "transforms/s", "h2d_bytes_per_step": bh.numel() * 8, "d2h_bytes_per_step": oh.numel() * 8,
+           "path": "batch.BatchedC2C graph replay on a pinned host batch copied in, spectra copied out"}
     line = base_line(METRIC, value, "transforms/s", world, args, ms, "f32",
                      {"workload": "10,000 complex64 c2c of uneven lengths (40% 7-smooth, 20% primes, 40% uniform "
                                   "in [16, 65536]) in one persistent launch from a CUDA graph",
@@ -420,7 +474,7 @@ def run_c3(args):
                  "accuracy": {"worst_rel_l2_vs_port_sampled": worst, "batched_vs_per_launch_rel_l2": diff},
                  "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "transforms/s", "cores": cores, "kind": "port",
                                   "sample": f"first 1000 rows of the batch, one call per row, {cores} threads"},
-                 "e2e": None, "gpu_launches": launches, "clocks": clocks})
+                 "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
