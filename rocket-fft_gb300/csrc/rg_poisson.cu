@@ -30,19 +30,75 @@ struct Grid {
   int64_t n0, n1, n2;
 };
 
+// Row sweep of the n0 x n1 x n2 grid (C order) for the elementwise and stencil kernels: a few
+// CTAs per SM; at step t CTA b takes the ROWS rows (k0, k1) number t * G * ROWS + u * G + b
+// (u < ROWS, G = gridDim.x), its threads run along the last axis, and the loads of all ROWS rows
+// are issued before any use. All CTAs move through the volume together, a window of G * ROWS
+// rows (a few planes), so a stencil's neighbours one plane away are recent L2 lines.
+// Row number u of step t for this CTA, and its (k0, k1).
+__device__ __forceinline__ int64_t sweep_row(int64_t t, int u, int rows_per_step) {
+  return (t * rows_per_step + u) * int64_t(gridDim.x) + blockIdx.x;
+}
+
 // Grid of the stencil-shaped kernels: x = positions along the last axis (blockDim.x threads
 // each), y = index along the middle axis, z = index along the first axis; no divisions.
 // X /= lambda in X's own precision: the float32 spectral solve of the mixed-precision
 // refinement only needs float accuracy, and GB300's FP64 rate would otherwise bound it (the
 // eigenvalues are all <= 0, so their sum has no cancellation).
-template <typename T>
-__global__ void __launch_bounds__(256) eigdiv_kernel(T *X, Grid g, const T *l0, const T *l1, const T *l2) {
-  const int64_t k2 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k2 >= g.n2) return;
-  const int64_t k1 = blockIdx.y, k0 = blockIdx.z;
-  const int64_t i = (k0 * g.n1 + k1) * g.n2 + k2;
-  const T lam = (l0[k0] + l1[k1]) + l2[k2];
-  X[i] = i == 0 ? T(0) : X[i] / lam;
+// V consecutive elements of a row per thread as one vector load/store (V = 16 / sizeof(T) when
+// the rows allow it, else 1), ROWS rows per step: enough bytes in flight per SM for the copy
+// bandwidth (an elementwise pass carries no reuse to hide latency with).
+template <typename T, int V> struct Vec;
+template <> struct Vec<float, 4> { using type = float4; };
+template <> struct Vec<double, 2> { using type = double2; };
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256, 4) eigdiv_kernel(T *X, Grid g, const T *l0, const T *l1, const T *l2) {
+  constexpr int ROWS = V == 1 ? 8 : 4;
+  const int64_t rows = g.n0 * g.n1;
+  for (int64_t t = 0; t * gridDim.x * ROWS < rows; ++t) {
+    T *base[ROWS];
+    T lam01[ROWS];
+#pragma unroll
+    for (int u = 0; u < ROWS; ++u) {
+      const int64_t row = sweep_row(t, u, ROWS);
+      base[u] = row < rows ? X + row * g.n2 : nullptr;
+      if (row < rows) {
+        const int64_t k0 = row / g.n1;
+        lam01[u] = l0[k0] + l1[row - k0 * g.n1];
+      }
+    }
+    for (int64_t k2 = int64_t(threadIdx.x) * V; k2 < g.n2; k2 += int64_t(blockDim.x) * V) {
+      T l2k[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) l2k[v] = l2[k2 + v];
+      if constexpr (V == 1) {
+        T x[ROWS];
+#pragma unroll
+        for (int u = 0; u < ROWS; ++u)
+          if (base[u]) x[u] = base[u][k2];
+#pragma unroll
+        for (int u = 0; u < ROWS; ++u)
+          if (base[u]) base[u][k2] = (base[u] == X && k2 == 0) ? T(0) : x[u] / (lam01[u] + l2k[0]);
+      } else {
+        using VT = typename Vec<T, V>::type;
+        VT x[ROWS];
+#pragma unroll
+        for (int u = 0; u < ROWS; ++u)
+          if (base[u]) x[u] = *reinterpret_cast<const VT *>(base[u] + k2);
+#pragma unroll
+        for (int u = 0; u < ROWS; ++u) {
+          if (base[u]) {
+            T *e = reinterpret_cast<T *>(&x[u]);
+#pragma unroll
+            for (int v = 0; v < V; ++v) e[v] = e[v] / (lam01[u] + l2k[v]);
+            if (base[u] == X && k2 == 0) e[0] = T(0);
+            *reinterpret_cast<VT *>(base[u] + k2) = x[u];
+          }
+        }
+      }
+    }
+  }
 }
 
 // r = f - A(u_hi + u_lo): the hi second differences (a - c) + (b - c) are exact for a smooth
@@ -200,6 +256,12 @@ unsigned grid_for(int64_t total) {
   return unsigned(std::min<int64_t>(b, 152 * 16));
 }
 
+// CTAs of the row-sweep kernels: a few per SM, at most one per row
+unsigned grid_rows(const Grid &g, int per_sm) {
+  const int64_t want = int64_t(rg::sm_count()) * per_sm;
+  return unsigned(std::max<int64_t>(1, std::min<int64_t>(want, g.n0 * g.n1)));
+}
+
 dim3 grid3(const Grid &g) {
   RG_CHECK(g.n1 < 65536 && g.n0 < 65536, RG_ERR_UNSUPPORTED, "grid extent beyond 65535 along the first two axes");
   return dim3(unsigned((g.n2 + 255) / 256), unsigned(g.n1), unsigned(g.n0));
@@ -218,15 +280,19 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_eigdiv(v
     RG_CHECK(n0 > 0 && n1 > 0 && n2 > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Grid g{n0, n1, n2};
-    const dim3 b = grid3(g);
+    const unsigned b = grid_rows(g, 4);
     const uint64_t bytes = uint64_t(2 * itemsize) * uint64_t(n0 * n1 * n2);
     rg::profiled_launch(itemsize == 4 ? "poisson_eigdiv_f32" : "poisson_eigdiv_f64", bytes, st, [&] {
+      // vector rows: n2 a multiple of the vector width and X 16-byte aligned
+      const bool vec = n2 % (16 / itemsize) == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0;
       if (itemsize == 4) {
         const float *l = static_cast<const float *>(lam);
-        eigdiv_kernel<float><<<b, 256, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
+        if (vec) eigdiv_kernel<float, 4><<<b, 256, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
+        else eigdiv_kernel<float, 1><<<b, 256, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
       } else {
         const double *l = static_cast<const double *>(lam);
-        eigdiv_kernel<double><<<b, 256, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
+        if (vec) eigdiv_kernel<double, 2><<<b, 256, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
+        else eigdiv_kernel<double, 1><<<b, 256, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
       }
     });
     rg::note_launch();
