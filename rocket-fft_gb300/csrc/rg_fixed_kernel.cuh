@@ -649,51 +649,47 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
     }
     __syncthreads();
     fx_middle<T, OP, E, COL, false, 0, NP>(a, row0, rows, buf, tw, scale, pair_ok);
-    // split Z_0..Z_{L-1} into X_0..X_L in place
+    // split and post-twiddle fused: the thread takes the pairs (k, L - k), k = first + q * TPR
+    // <= L / 2, of its row, forms X_k and X_{L-k} from Z_k and Z_{L-k} and stores the four
+    // outputs they give: with z = t_k X_k, y_k = 2 Re z and y_{N-k} = -2 Im z (t_{N-k} =
+    // -i conj t_k), the same for L - k; k = 0 gives y_0 and y_L from X_0 = Re Z_0 + Im Z_0 and
+    // X_L = Re Z_0 - Im Z_0 (both real). Output position p = kk (DCT) or N-1-kk (DST); y at p = 0
+    // weighted e0.
     {
-      const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux2);
-      constexpr int HALF = L / 2 + 1;
-      for (int e = tid; e < rows * HALF; e += NT) {
-        const int r = e / HALF;
-        const int k = e - r * HALF;
-        cx<T> *row = buf + r * PITCH;
-        if (k == 0) {
-          const cx<T> z0 = row[0];
-          row[0] = mk<T>(z0.x + z0.y, T(0));
-          row[L + (L >> PS)] = mk<T>(z0.x - z0.y, T(0));
-        } else {
-          const int kc = L - k;
-          const cx<T> zk = row[k + (k >> PS)], zc = cj<T>(row[kc + (kc >> PS)]);
-          const cx<T> Ev = scl<T>(add<T>(zk, zc), T(0.5));
-          const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
-          const cx<T> u = mul<T>(__ldg(w + k), O);
-          row[k + (k >> PS)] = add<T>(Ev, u);
-          if (kc != k) row[kc + (kc >> PS)] = cj<T>(sub<T>(Ev, u));
-        }
-      }
-    }
-    __syncthreads();
-    // post-twiddle and store
-    {
-      constexpr int NQ = (N + TPR - 1) / TPR;
+      constexpr int HP2 = L / 2 + 1, NQ = (HP2 + TPR - 1) / TPR;
       const int64_t so = a.st.axis_stride;
-      const T fct = T(a.fct), e0 = T(a.e0);
-      const cx<T> *t2 = reinterpret_cast<const cx<T> *>(a.aux);  // e^{-i pi k / 2n}, k < n
+      const T fct2 = T(2) * T(a.fct), e0 = T(a.e0);
+      const cx<T> *t2 = reinterpret_cast<const cx<T> *>(a.aux);   // e^{-i pi k / 2n}, k <= L used
+      const cx<T> *w = reinterpret_cast<const cx<T> *>(a.aux2);    // W_n^k, k <= L / 2
       if (sr < rows) {
         T *p = reinterpret_cast<T *>(a.out) + side_offset32(a.st, row0 + uint32_t(sr));
         const cx<T> *row = buf + sr * PITCH;
-#pragma unroll 4
+        auto put = [&](int kk, T y) {
+          const int pos = sine ? N - 1 - kk : kk;
+          p[pos * so] = pos == 0 ? y * e0 : y;
+        };
+        auto emit = [&](int k, cx<T> X) {  // 0 < k < L
+          const cx<T> z = mul<T>(__ldg(t2 + k), X);
+          put(k, z.x * fct2);
+          put(N - k, -z.y * fct2);
+        };
+#pragma unroll 2
         for (int q = 0; q < NQ; ++q) {
-          const int pos = si0 + q * TPR;
-          if (N % TPR == 0 || pos < N) {
-            const int kk = sine ? N - 1 - pos : pos;
-            const int kx = kk <= L ? kk : N - kk;
-            cx<T> X = row[kx + (kx >> PS)];
-            if (kk > L) X.y = -X.y;
-            const cx<T> t = __ldg(t2 + kk);
-            T y = T(2) * (X.x * t.x - X.y * t.y) * fct;
-            if (pos == 0) y *= e0;
-            p[pos * so] = y;
+          const int k = si0 + q * TPR;
+          if (HP2 % TPR == 0 || k < HP2) {
+            if (k == 0) {
+              const cx<T> z0 = row[0];
+              put(0, (z0.x + z0.y) * fct2);
+              put(L, (z0.x - z0.y) * __ldg(t2 + L).x * fct2);
+            } else {
+              const int kc = L - k;
+              const cx<T> zk = row[k + (k >> PS)], zc = cj<T>(row[kc + (kc >> PS)]);
+              const cx<T> Ev = scl<T>(add<T>(zk, zc), T(0.5));
+              const cx<T> O = mnegi<T>(scl<T>(sub<T>(zk, zc), T(0.5)));
+              const cx<T> u = mul<T>(__ldg(w + k), O);
+              emit(k, add<T>(Ev, u));
+              if (kc != k) emit(kc, cj<T>(sub<T>(Ev, u)));
+            }
           }
         }
       }
