@@ -102,3 +102,26 @@ def test_fftlog_argument_validation(F):
             F.fhtoffset(1.0, 1.0, bad)
         with pytest.raises(TypeError, match="bias"):
             F.fhtoffset(1.0, 1.0, 1.0, bad)
+
+
+def test_roll_typing(rg):
+    """numpy.roll argument rules of the reference's overload (tests/test_misc.py TestRollTyping):
+    shift and axis integers / booleans, scalar or one-dimensional; a string is not array-like;
+    scalars come back as 0-d arrays."""
+    R = rg.numpy_fft.roll
+    x = np.arange(10)
+    for bad in (None, 1.0, ((1,),)):
+        with pytest.raises(TypeError, match="shift"):
+            R(x, shift=bad)
+    with pytest.raises(AttributeError):
+        R(x, shift=np.array([[1]]), axis=np.array([0]))
+    for bad in (1.0, ((1,),)):
+        with pytest.raises(TypeError, match="axis"):
+            R(x, shift=1, axis=bad)
+    with pytest.raises(AttributeError):
+        R(x, shift=np.array([1]), axis=np.array([[0]]))
+    with pytest.raises(TypeError):
+        R("abc", shift=1)
+    with pytest.raises(TypeError):
+        R(x)
+    assert R(42.0, 1) == np.asarray(42.0) and R(True, 1) == np.asarray(True)

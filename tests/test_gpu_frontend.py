@@ -239,3 +239,51 @@ def test_fht_singular(rg, cuda, n):
     with pytest.warns(UserWarning, match="singular inverse"):
         back = rg.fft.ifht(torch.from_numpy(A).cuda(), dln, 1.0, bias=2.0)
     assert oracle.rel_l2(back.cpu().numpy(), fftlog.ifht(A, dln, 1.0, 0.0, 2.0)) <= _fht_tol(n, dln, 2.0)
+
+
+ROLL_CASES = [
+    # shape, shift, axis
+    ((10,), 2, None),
+    ((2, 5), 1, None),
+    ((2, 5), 1, 0),
+    ((2, 5), 1, 1),
+    ((2, 5), 1, (0, 1)),
+    ((2, 5), (-1, -1), (0, 1)),
+    ((2, 5), 1, (1, 1)),        # the same axis twice
+    ((2, 5), 6, 1),             # more than one turn
+    ((2, 5), -4, 1),
+    ((0,), 1, 0),
+    ((1,), -1, 0),
+    ((83,), 21, (0,)),
+    ((83,), -21, None),
+    ((3, 42, 42), (-12, 85, 1), (-3, 1, 0)),
+    ((99, 50, 25), (5, 2), (0, 0)),
+    ((100, 3, 19, 19), (3, 3), (2, 3)),
+    ((2, 5), (1, 0), None),     # several shifts of the flattened array
+]
+
+
+def _layouts(a):
+    yield "C", np.ascontiguousarray(a)
+    yield "F", np.asfortranarray(a)
+    big = np.random.default_rng(1).random(tuple(2 * n for n in a.shape)) if a.size else a
+    yield "strided", big[tuple(slice(None, None, 2) for _ in a.shape)] if a.size else a
+
+
+@pytest.mark.parametrize("shape,shift,axis", ROLL_CASES)
+def test_numpy_roll(rg, cuda, shape, shift, axis):
+    """numpy.roll of the reference's overload (overloads.py:762-855, tests/test_misc.py):
+    bit-exact against np.roll on NumPy inputs of C, F and strided layout (same dtype and
+    contiguity flags) and on device tensors."""
+    torch = cuda
+    base = np.random.default_rng(2).random(shape)
+    for name, a in _layouts(base):
+        got = rg.numpy_fft.roll(a, shift, axis)
+        want = np.roll(a, shift, axis)
+        assert np.array_equal(got, want), name
+        assert got.dtype == want.dtype
+        assert got.flags.c_contiguous == want.flags.c_contiguous, name
+        assert got.flags.f_contiguous == want.flags.f_contiguous, name
+    ints = np.arange(int(np.prod(shape))).reshape(shape)
+    td = torch.from_numpy(ints).cuda()
+    assert np.array_equal(rg.numpy_fft.roll(td, shift, axis).cpu().numpy(), np.roll(ints, shift, axis))
