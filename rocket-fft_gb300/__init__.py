@@ -39,5 +39,11 @@ from .pocketfft import (  # noqa: F401
 )
 
 from . import fft, numpy_fft  # noqa: F401,E402  (SciPy/NumPy-level front ends)
+from .fft import get_workers, numpy_like, scipy_like, set_workers  # noqa: F401,E402
+
+# the reference's short names (rocket_fft/__init__.py:30-32)
+separable_hartley = r2r_separable_hartley
+genuine_hartley = r2r_genuine_hartley
+fftpack = r2r_fftpack
 
 __version__ = "0.1.0"

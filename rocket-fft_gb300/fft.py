@@ -135,7 +135,54 @@ def _wrap_axis(ax, ndim):
     return ax + ndim if ax < 0 else ax
 
 
-def _shape_and_axes(x, s, axes, unique=True):
+# NumPy allows an axis to repeat in fft2/fftn/ifft2/ifftn (and the other N-d functions), SciPy
+# does not. The reference makes the rule process-wide for both interfaces
+# (rocket_fft/overloads.py:333-338, 387-405): SciPy-like when SciPy is installed (its default),
+# NumPy-like otherwise, switched by scipy_like() / numpy_like().
+try:
+    import scipy as _scipy  # noqa: F401
+
+    _unique_axes = True
+except ImportError:  # pragma: no cover
+    _unique_axes = False
+
+
+def scipy_like():
+    """Repeated axes are an error in every N-d transform of both interfaces (SciPy's rule)."""
+    global _unique_axes
+    _unique_axes = True
+
+
+def numpy_like():
+    """Repeated axes are transformed again in every N-d transform of both interfaces (NumPy's
+    rule)."""
+    global _unique_axes
+    _unique_axes = False
+
+
+_workers = 1
+
+
+def get_workers():
+    """The default `workers` value (the reference's rocket_fft.get_workers; the GPU grid does
+    the work, the value is only recorded)."""
+    return _workers
+
+
+def set_workers(workers):
+    """Set the default `workers` value; 1 <= workers <= CPU count, as the reference checks."""
+    global _workers
+    import os
+
+    workers = int(workers)
+    if workers < 1:
+        raise ValueError("Number of workers cannot be smaller than one.")
+    if workers > (os.cpu_count() or 1):
+        raise ValueError(f"Number of workers exceeds CPU count of {os.cpu_count()}.")
+    _workers = workers
+
+
+def _shape_and_axes(x, s, axes, unique=None):
     ndim = x.ndim
     if s is not None:
         s = [int(v) for v in np.atleast_1d(np.asarray(s, dtype=np.int64))]
@@ -151,7 +198,7 @@ def _shape_and_axes(x, s, axes, unique=True):
             axes = list(range(ndim - len(s), ndim))
     else:
         axes = [_wrap_axis(a, ndim) for a in np.atleast_1d(np.asarray(axes, dtype=np.int64))]
-    if unique and len(set(axes)) != len(axes):
+    if (_unique_axes if unique is None else unique) and len(set(axes)) != len(axes):
         raise ValueError("All axes must be unique.")
     if s is not None and len(s) != len(axes):
         raise ValueError("When given, axes and shape arguments have to be of the same length.")
@@ -206,7 +253,7 @@ def _axes_arg(axes):
 # generic transforms (rocket_fft/overloads.py:943-1045)
 # ---------------------------------------------------------------------------------------------
 
-def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=True):
+def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=None):
     x = _asarray(x)
     s, axes = _shape_and_axes(x, s, axes, unique)
     shape = list(x.shape)
@@ -227,7 +274,7 @@ def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=True):
     return out
 
 
-def _r2cn(x, s, axes, norm, forward, unique=True):
+def _r2cn(x, s, axes, norm, forward, unique=None):
     x = _asarray(x)
     if _kind(x) == "c":
         raise TypeError("x must be a real sequence")
@@ -245,7 +292,7 @@ def _r2cn(x, s, axes, norm, forward, unique=True):
     return out
 
 
-def _c2rn(x, s, axes, norm, forward, unique=True):
+def _c2rn(x, s, axes, norm, forward, unique=None):
     x = _asarray(x)
     s, axes = _shape_and_axes(x, s, axes, unique)
     last = axes[-1]

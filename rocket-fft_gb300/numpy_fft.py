@@ -1,7 +1,8 @@
 """``numpy.fft`` on the GPU transform path (the NumPy overloads of rocket-fft,
-rocket_fft/overloads.py:1043-1310): the same transforms as :mod:`fft` with NumPy's rules -- axes
-may repeat (a repeated axis is transformed again, as NumPy and the reference do), and ``out``,
-when given, receives the result (it must have the result's shape and dtype). Also ``roll``,
+rocket_fft/overloads.py:1043-1310): the same transforms as :mod:`fft` with NumPy's argument
+rules, ``out`` (when given) receiving the result (it must have the result's shape and dtype).
+Whether an axis may repeat follows the process-wide rule of ``numpy_like()`` / ``scipy_like()``
+(SciPy-like by default when SciPy is installed, as in the reference). Also ``roll``,
 numpy.roll, which the reference overloads beside them (overloads.py:762-855) and which
 fftshift/ifftshift are made of.
 """
@@ -32,64 +33,64 @@ def _out(res, out):
 
 def fft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2cn(a, s, axes, norm, False, True, unique=False), out)
+    return _out(_f._c2cn(a, s, axes, norm, False, True), out)
 
 
 def ifft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2cn(a, s, axes, norm, False, False, unique=False), out)
+    return _out(_f._c2cn(a, s, axes, norm, False, False), out)
 
 
 def fft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, True, unique=False), out)
+    return _out(_f._c2cn(a, s, axes, norm, False, True), out)
 
 
 def ifft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, False, unique=False), out)
+    return _out(_f._c2cn(a, s, axes, norm, False, False), out)
 
 
 def fftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, True, unique=False), out)
+    return _out(_f._c2cn(a, s, axes, norm, False, True), out)
 
 
 def ifftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, False, unique=False), out)
+    return _out(_f._c2cn(a, s, axes, norm, False, False), out)
 
 
 def rfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._r2cn(a, s, axes, norm, True, unique=False), out)
+    return _out(_f._r2cn(a, s, axes, norm, True), out)
 
 
 def irfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2rn(a, s, axes, norm, False, unique=False), out)
+    return _out(_f._c2rn(a, s, axes, norm, False), out)
 
 
 def rfft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._r2cn(a, s, axes, norm, True, unique=False), out)
+    return _out(_f._r2cn(a, s, axes, norm, True), out)
 
 
 def irfft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._c2rn(a, s, axes, norm, False, unique=False), out)
+    return _out(_f._c2rn(a, s, axes, norm, False), out)
 
 
 def rfftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._r2cn(a, s, axes, norm, True, unique=False), out)
+    return _out(_f._r2cn(a, s, axes, norm, True), out)
 
 
 def irfftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._c2rn(a, s, axes, norm, False, unique=False), out)
+    return _out(_f._c2rn(a, s, axes, norm, False), out)
 
 
 def hfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2rn(a, s, axes, norm, True, unique=False), out)
+    return _out(_f._c2rn(a, s, axes, norm, True), out)
 
 
 def ihfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._r2cn(a, s, axes, norm, False, unique=False), out)
+    return _out(_f._r2cn(a, s, axes, norm, False), out)
 
 
 fftfreq = _f.fftfreq

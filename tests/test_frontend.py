@@ -125,3 +125,25 @@ def test_roll_typing(rg):
     with pytest.raises(TypeError):
         R(x)
     assert R(42.0, 1) == np.asarray(42.0) and R(True, 1) == np.asarray(True)
+
+
+def test_interface_switches(rg):
+    """scipy_like() / numpy_like() (the reference's rocket_fft namespace, overloads.py:333-338):
+    SciPy-like by default when SciPy is installed, repeated axes then rejected by the N-d
+    functions of both interfaces; get_workers / set_workers with the reference's checks; the
+    reference's short names for the r2r functions."""
+    x = np.ones((3, 3, 3))
+    for fn in (rg.fft.fftn, rg.fft.ifft2, rg.numpy_fft.fftn, rg.numpy_fft.ifft2, rg.fft.dctn, rg.fft.rfftn):
+        with pytest.raises(ValueError, match="unique"):
+            fn(x, axes=(0, 0))
+    assert rg.get_workers() == 1
+    with pytest.raises(ValueError):
+        rg.set_workers(0)
+    import os
+
+    with pytest.raises(ValueError):
+        rg.set_workers((os.cpu_count() or 1) + 1)
+    rg.set_workers(1)
+    assert rg.separable_hartley is rg.r2r_separable_hartley
+    assert rg.genuine_hartley is rg.r2r_genuine_hartley
+    assert rg.fftpack is rg.r2r_fftpack

@@ -150,7 +150,11 @@ def test_numpy_namespace(rg, cuda):
     torch = cuda
     x = _rand((6, 10), np.complex128, 7)
     xd = torch.from_numpy(x).cuda()
-    _cmp(rg.numpy_fft.fftn(xd, axes=(1, 1)), np.fft.fftn(x, axes=(1, 1)), np.complex128)  # repeated axis
+    rg.numpy_like()
+    try:
+        _cmp(rg.numpy_fft.fftn(xd, axes=(1, 1)), np.fft.fftn(x, axes=(1, 1)), np.complex128)  # repeated axis
+    finally:
+        rg.scipy_like()
     out = torch.empty_like(xd)
     res = rg.numpy_fft.ifft2(xd, out=out)
     assert res is out
@@ -287,3 +291,101 @@ def test_numpy_roll(rg, cuda, shape, shift, axis):
     ints = np.arange(int(np.prod(shape))).reshape(shape)
     td = torch.from_numpy(ints).cuda()
     assert np.array_equal(rg.numpy_fft.roll(td, shift, axis).cpu().numpy(), np.roll(ints, shift, axis))
+
+
+def test_overwrite_and_dtype(rg, cuda):
+    """overwrite_x and result dtypes as the reference's tests/test_overwrite_and_dtype.py: with
+    overwrite_x the input itself is the result when it already has the transform's dtype and
+    shape (c2c, dct of real and of complex input), never for r2c / c2r / real-input fft;
+    integer, bool and byte inputs become float64 / complex128, single precision stays single;
+    complex input to rfft is rejected. Checked on NumPy arrays and on device tensors."""
+    torch = cuda
+    F = rg.fft
+    rng = np.random.default_rng(3)
+
+    def arr(dtype, dev):
+        x = rng.random(42).astype(dtype)
+        return torch.from_numpy(x).cuda() if dev else x
+
+    def dt(y):
+        return np.dtype(str(y.dtype).replace("torch.", "")) if hasattr(y, "is_cuda") else y.dtype
+
+    for dev in (False, True):
+        # r2r
+        x = arr(np.float64, dev); y = F.dct(x); assert y is not x and dt(y) == np.float64
+        x = arr(np.float64, dev); assert F.dct(x, overwrite_x=True) is x
+        if not dev:
+            x = arr(np.byte, dev); y = F.dct(x); assert y is not x and dt(y) == np.float64
+        x = arr(np.float32, dev); y = F.dct(x, overwrite_x=True); assert y is x and dt(y) == np.float32
+        x = arr(np.complex128, dev); y = F.dct(x); assert y is not x and dt(y) == np.complex128
+        x = arr(np.complex64, dev); y = F.dct(x, overwrite_x=True); assert y is x and dt(y) == np.complex64
+        # c2r
+        for t, want in ((np.complex128, np.float64), (np.complex64, np.float32), (np.float64, np.float64)):
+            x = arr(t, dev); y = F.irfft(x); assert y is not x and dt(y) == want
+            x = arr(t, dev); assert F.irfft(x, overwrite_x=True) is not x
+        # r2c
+        x = arr(np.float64, dev); y = F.rfft(x); assert y is not x and dt(y) == np.complex128
+        x = arr(np.float64, dev); assert F.rfft(x, overwrite_x=True) is not x
+        if not dev:
+            x = arr(np.int16, dev); y = F.rfft(x, overwrite_x=True); assert y is not x and dt(y) == np.complex128
+        with pytest.raises(TypeError):
+            F.rfft(arr(np.complex128, dev), overwrite_x=True)
+        # c2c
+        for t in (np.complex128, np.complex64):
+            x = arr(t, dev); y = F.fft(x); assert y is not x and dt(y) == t
+            x = arr(t, dev); assert F.fft(x, overwrite_x=True) is x
+        # c2c_sym (real input)
+        x = arr(np.float64, dev); y = F.fft(x); assert y is not x and dt(y) == np.complex128
+        x = arr(np.float64, dev); assert F.fft(x, overwrite_x=True) is not x
+        if not dev:
+            x = arr(np.bool_, dev); y = F.fft(x, overwrite_x=True); assert y is not x and dt(y) == np.complex128
+
+
+LIKE_AXES = [(0, 0), (0, 2, 2), (0, 2, 1, 0), (3, 1), (2, 1, 0), (0, 1, 2, 3)]
+
+
+def _outcome(fn, x, axes):
+    try:
+        return fn(x, axes=axes), False
+    except Exception:
+        return None, True
+
+
+@pytest.mark.parametrize("mode", ["scipy", "numpy"])
+def test_like_interfaces(rg, cuda, mode):
+    """The reference's tests/test_scipy_like.py / test_numpy_like.py: under scipy_like() the N-d
+    functions raise exactly where SciPy raises (repeated axes) and agree with it elsewhere; under
+    numpy_like() they agree with NumPy for every axes tuple, repeated axes included."""
+    x = np.random.default_rng(9).random((3, 3, 3, 3)).astype(np.complex128)
+    ref = sfft if mode == "scipy" else np.fft
+    ours = rg.fft if mode == "scipy" else rg.numpy_fft
+    (rg.scipy_like if mode == "scipy" else rg.numpy_like)()
+    try:
+        for name in ("fft2", "fftn", "ifft2", "ifftn"):
+            for axes in LIKE_AXES:
+                got, raised = _outcome(getattr(ours, name), x, axes)
+                want, ref_raised = _outcome(getattr(ref, name), x, axes)
+                assert raised == ref_raised, (mode, name, axes)
+                if not raised:
+                    assert oracle.rel_l2(np.asarray(got), want) <= 1e-13, (mode, name, axes)
+    finally:
+        rg.scipy_like()
+
+
+LIKE_DTYPES = [np.complex64, np.complex128, np.float32, np.float64, np.int8, np.int16, np.int32, np.int64,
+               np.uint8, np.uint16, np.uint32, np.uint64, np.bool_]
+
+
+def test_like_dtypes(rg, cuda):
+    """Result dtypes for every input type of the reference's table (overloads.py:48-63) equal
+    SciPy's (fft, dct, fht, ifht, fhtoffset) and NumPy's (fft)."""
+    x = np.random.default_rng(10).random(42)
+    for ty in LIKE_DTYPES:
+        a = x.astype(ty)
+        assert rg.fft.fft(a).dtype == sfft.fft(a).dtype, ty
+        assert rg.fft.dct(a).dtype == sfft.dct(a).dtype, ty
+        assert rg.numpy_fft.fft(a).dtype == np.fft.fft(a).dtype, ty
+        if not np.issubdtype(ty, np.complexfloating):
+            one = ty(1) if ty is not np.bool_ else 1.0
+            assert rg.fft.fht(a, one, one).dtype == sfft.fht(a, one, one).dtype, ty
+            assert rg.fft.ifht(a, one, one).dtype == sfft.ifht(a, one, one).dtype, ty
