@@ -114,3 +114,25 @@ def test_fftw_dct_dst_on_gpu(rg, cuda, rdt, fname):
         assert e <= (1e-5 if rdt == np.float32 else 1e-12), (key, e)
         checked += 1
     assert checked > 0
+
+
+LARGE = [8193, 10007, 2**14 * 3, 65521, 65536, 3**10, 2**20, 1000003]
+
+
+@pytest.mark.parametrize("cdt", [np.complex128, np.complex64])
+def test_c2c_large_lengths(rg, cuda, cdt):
+    """Lengths past one CTA: four-step for smooth lengths (2^16, 3^10, 3 * 2^14, 2^20) and
+    Bluestein through a workspace for large primes (8193 = 3 * 2731, 10007, 65521, 1000003)."""
+    torch = cuda
+    rng = np.random.default_rng(43)
+    P = oracle.port()
+    ax = np.array([0], np.int64)
+    for n in LARGE:
+        x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(cdt)
+        want = np.empty(n, np.complex128)
+        P.c2c(x.astype(np.complex128), want, [0], True, 1.0, 8)
+        xd = torch.from_numpy(x).cuda()
+        X = torch.empty_like(xd)
+        rg.c2c(xd, X, ax, True, 1.0, 1)
+        e = oracle.rel_l2(X.cpu().numpy(), want)
+        assert e <= TOL[np.dtype(cdt)], (n, e)
