@@ -156,6 +156,12 @@ int rocketgpu_poisson_to_fx(const double *f, int32_t e, int64_t *F, float *Frem,
 int rocketgpu_poisson_residual_fx(const int64_t *U, const int64_t *F, const float *Frem, int32_t e, int32_t k,
                                   float *r32, int64_t n0, int64_t n1, int64_t n2, double *sumsq, void *stream);
 int rocketgpu_poisson_fx_to_double(const int64_t *U, int32_t e, double *out, int64_t total, void *stream);
+/* out = (U - m) 2^-e with m = the mean of U rounded to an integer (exact 128-bit sum): the
+ * zero-mean solution, without FP64 arithmetic per element. Workspace from the library's pool. */
+int rocketgpu_poisson_fx_to_double_zero_mean(const int64_t *U, int32_t e, double *out, int64_t total, void *stream);
+/* *out (device double) = max |x| over total float32 (itemsize 4) or float64 (8) elements of a
+ * device array, by integer comparison of the bits. */
+int rocketgpu_abs_max(const void *x, int64_t itemsize, int64_t total, double *out, void *stream);
 const char *rocketgpu_poisson_last_error(void);
 
 /* ---- batched uneven-length complex FFTs (no reference counterpart) ----

@@ -17,11 +17,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/rocket_gpu.h"
 #include "rg_error.hpp"
+#include "rg_exec.hpp"
 #include "rg_launch.hpp"
 
 namespace {
@@ -218,21 +221,164 @@ __global__ void __launch_bounds__(256) fx_residual_kernel(const long long *U, co
   }
 }
 
-// F = round(f * 2^e), Frem = f - F 2^-e (exact in double, stored as float)
+// The conversions between float64 and the fixed-point scale run on integer arithmetic over the
+// bits of the doubles: GB300's FP64 pipe made the plain double versions (ldexp, rounding,
+// subtraction, int64 <-> double conversions) the most expensive kernels of a solve.
+
+// F = round(f 2^e) (half to even) and Frem = f - F 2^-e rounded to float, from the exponent and
+// mantissa of f (|f| = M 2^ex): f 2^e = M 2^s, s = ex + e; for s < 0 the quotient M >> -s is
+// rounded and the remainder r (|r| <= 2^(-s-1)) is exact, Frem = +-r 2^ex. Same values as
+// __double2ll_rn(ldexp(f, e)) and float(f - ldexp(double(F), -e)) (that difference is exact).
+// v 2^ex as a float rounded to nearest even, assembled from the normalised magnitude of v
+// (correctly rounded, unlike the two-step ll_to_float); out of the normal range: ldexpf.
+__device__ __forceinline__ float scaled_float(long long v, int ex) {
+  if (v == 0) return 0.f;
+  const unsigned sgn = v < 0 ? 0x80000000u : 0u;
+  unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll((long long)a);
+  a <<= lz;  // top bit at 63: |v| = a 2^-lz
+  unsigned long long mant = a >> 40;
+  const unsigned long long rb = a & ((1ull << 40) - 1), half = 1ull << 39;
+  if (rb > half || (rb == half && (mant & 1ull))) ++mant;
+  int E = 63 - lz + ex;  // |v| 2^ex = mant 2^(E - 23)
+  if (mant >> 24) {
+    mant >>= 1;
+    ++E;
+  }
+  const int biased = E + 127;
+  if (biased <= 0 || biased >= 255) return ldexpf(ll_to_float(v), ex);
+  return __uint_as_float(sgn | unsigned(biased) << 23 | unsigned(mant & 0x7fffffull));
+}
+
+__device__ __forceinline__ void fixed_of(double f, int e, long long &F, float &rem) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(f);
+  const bool neg = (b >> 63) != 0;
+  const int E = int((b >> 52) & 0x7ffull);
+  unsigned long long M = b & 0xfffffffffffffull;
+  if (E != 0) M |= 1ull << 52;
+  const int ex = (E != 0 ? E : 1) - 1075;
+  const int s = ex + e;
+  unsigned long long Fm = 0;
+  long long r = 0;
+  if (M != 0) {
+    if (s >= 0) {
+      Fm = M << s;  // exact; the caller keeps |F| < 2^62
+    } else if (s <= -64) {
+      r = (long long)M;  // M < 2^53 <= half of 2^-s: rounds to 0
+    } else {
+      const int t = -s;
+      const unsigned long long q = M >> t, low = M & ((1ull << t) - 1), half = 1ull << (t - 1);
+      const bool up = low > half || (low == half && (q & 1ull));
+      Fm = q + (up ? 1ull : 0ull);
+      r = (long long)(low - (up ? (1ull << t) : 0ull));  // two's complement: low - 2^t when up
+    }
+  }
+  F = neg ? -(long long)Fm : (long long)Fm;
+  rem = M == 0 ? (neg ? -0.f : 0.f) : scaled_float(neg ? -r : r, ex);  // -0.0 - 0.0 keeps its sign
+}
+
 __global__ void __launch_bounds__(256) fx_from_double_kernel(const double *f, long long *F, float *Frem, int64_t total,
                                                              int e) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    const long long v = __double2ll_rn(ldexp(f[i], e));
+    long long v;
+    float rem;
+    fixed_of(f[i], e, v, rem);
     F[i] = v;
-    if (Frem) Frem[i] = float(f[i] - ldexp(double(v), -e));
+    if (Frem) Frem[i] = rem;
   }
 }
 
-// out = U * 2^-e
-__global__ void __launch_bounds__(256) fx_to_double_kernel(const long long *U, double *out, int64_t total,
-                                                           double inv_scale) {
+// v 2^-e as a double rounded to nearest even, assembled from the normalised magnitude of v
+// (no FP64 operations); results outside the normal range fall back to the double path.
+__device__ __forceinline__ double scaled_double(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll((long long)a);
+  a <<= lz;  // top bit at 63: |v| = a 2^-lz
+  unsigned long long mant = a >> 11;
+  const unsigned long long rb = a & 0x7ffull;
+  if (rb > 0x400ull || (rb == 0x400ull && (mant & 1ull))) ++mant;
+  int E = 63 - lz - e;  // |v| 2^-e = mant 2^(E - 52)
+  if (mant >> 53) {
+    mant >>= 1;
+    ++E;
+  }
+  const int biased = E + 1023;
+  if (biased <= 0 || biased >= 2047) return ldexp(double(v), -e);
+  return __longlong_as_double((long long)(sgn | (unsigned long long)biased << 52 | (mant & 0xfffffffffffffull)));
+}
+
+// out = (U - *m) 2^-e (m = 0 when NULL)
+__global__ void __launch_bounds__(256) fx_to_double_kernel(const long long *U, double *out, int64_t total, int e,
+                                                           const long long *m) {
+  const long long shift = m ? *m : 0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
-    out[i] = double(U[i]) * inv_scale;
+    out[i] = scaled_double(U[i] - shift, e);
+}
+
+// Exact sum of the int64 iterate (128-bit accumulators), one partial per CTA.
+__global__ void __launch_bounds__(256) fx_sum_kernel(const long long *U, int64_t total, unsigned long long *part) {
+  __int128 acc = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
+    acc += U[i];
+  __shared__ __int128 sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (int(threadIdx.x) < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const unsigned __int128 v = (unsigned __int128)sh[0];
+    part[2 * blockIdx.x] = (unsigned long long)v;
+    part[2 * blockIdx.x + 1] = (unsigned long long)(v >> 64);
+  }
+}
+
+// m = the mean of U rounded to an integer (the division in double: within one unit of the
+// exact rounding, 2^-e of the solution)
+__global__ void fx_mean_kernel(const unsigned long long *part, int nparts, int64_t total, long long *m) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __int128 S = 0;
+  for (int b = 0; b < nparts; ++b)
+    S += (__int128)(((unsigned __int128)part[2 * b + 1] << 64) | (unsigned __int128)part[2 * b]);
+  const double hi = double((long long)(S >> 64)), lo = double((unsigned long long)S);
+  *m = (long long)llrint((hi * 18446744073709551616.0 + lo) / double(total));
+}
+
+// max |x| over the bits (sign cleared, finite values order like their magnitudes), atomically
+// into *out as the bits of a double
+template <typename T>
+__global__ void __launch_bounds__(256) absmax_kernel(const T *x, int64_t total, unsigned long long *out) {
+  using B = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned>::type;
+  constexpr B mask = B(~B(0)) >> 1;
+  B mx = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    B b;
+    memcpy(&b, x + i, sizeof(B));
+    b &= mask;
+    mx = b > mx ? b : mx;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const B y = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = y > mx ? y : mx;
+  }
+  __shared__ B red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < int(blockDim.x >> 5); ++w) mx = red[w] > mx ? red[w] : mx;
+    unsigned long long d;
+    if constexpr (sizeof(T) == 8) {
+      d = mx;
+    } else {
+      float fv;
+      memcpy(&fv, &mx, 4);
+      d = (unsigned long long)__double_as_longlong(double(fv));
+    }
+    atomicMax(out, d);
+  }
 }
 
 thread_local std::string t_err;
@@ -383,8 +529,44 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_fx_to_do
   return guarded([&] {
     RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    fx_to_double_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<const long long *>(U), out, total,
-                                                         std::ldexp(1.0, -e));
+    fx_to_double_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<const long long *>(U), out, total, e,
+                                                         nullptr);
+    rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_fx_to_double_zero_mean(const int64_t *U,
+                                                                                              int32_t e, double *out,
+                                                                                              int64_t total,
+                                                                                              void *stream) {
+  return guarded([&] {
+    RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const unsigned g = grid_for(total);
+    rg::DevBuf work(size_t(2 * g + 1) * sizeof(unsigned long long), st);
+    unsigned long long *part = static_cast<unsigned long long *>(work.get());
+    long long *m = reinterpret_cast<long long *>(part + 2 * g);
+    const long long *u = reinterpret_cast<const long long *>(U);
+    fx_sum_kernel<<<g, 256, 0, st>>>(u, total, part);
+    fx_mean_kernel<<<1, 32, 0, st>>>(part, int(g), total, m);
+    fx_to_double_kernel<<<g, 256, 0, st>>>(u, out, total, e, m);
+    for (int i = 0; i < 3; ++i) rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_abs_max(const void *x, int64_t itemsize, int64_t total,
+                                                                       double *out, void *stream) {
+  return guarded([&] {
+    RG_CHECK(itemsize == 4 || itemsize == 8, RG_ERR_ARG, "float32 or float64 data");
+    RG_CHECK(total >= 0, RG_ERR_ARG, "negative size");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RG_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
+    if (total == 0) return;
+    unsigned long long *o = reinterpret_cast<unsigned long long *>(out);
+    if (itemsize == 8) absmax_kernel<double><<<grid_for(total), 256, 0, st>>>(static_cast<const double *>(x), total, o);
+    else absmax_kernel<float><<<grid_for(total), 256, 0, st>>>(static_cast<const float *>(x), total, o);
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });

@@ -56,6 +56,10 @@ def _bind():
         lib.rocketgpu_poisson_residual_fx.restype = ctypes.c_int
         lib.rocketgpu_poisson_fx_to_double.argtypes = [P, i32, P, i64, P]
         lib.rocketgpu_poisson_fx_to_double.restype = ctypes.c_int
+        lib.rocketgpu_poisson_fx_to_double_zero_mean.argtypes = [P, i32, P, i64, P]
+        lib.rocketgpu_poisson_fx_to_double_zero_mean.restype = ctypes.c_int
+        lib.rocketgpu_abs_max.argtypes = [P, i64, i64, P, P]
+        lib.rocketgpu_abs_max.restype = ctypes.c_int
         lib._poisson_bound = True
     return lib
 
@@ -77,7 +81,14 @@ class NeumannPoisson:
         self.lam = torch.from_numpy(lam).to(self.dev)
         self.lam32 = self.lam.to(torch.float32)
         self.sumsq = torch.empty(1, dtype=torch.float64, device=self.dev)
+        self.amax = torch.empty(1, dtype=torch.float64, device=self.dev)
         self.lib = _bind()
+
+    def absmax(self, x):
+        """max |x| of a device float32/float64 array (integer comparisons of the bits)."""
+        _check(self.lib, self.lib.rocketgpu_abs_max(x.data_ptr(), x.element_size(), x.numel(), self.amax.data_ptr(),
+                                                     self._stream()))
+        return float(self.amax.item())
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
@@ -139,14 +150,14 @@ class NeumannPoisson:
             Frem = torch.empty(self.shape, dtype=torch.float32, device=self.dev)
             e = 0
             n = U.numel()
-            fmax = float(f.abs().max().item())
+            fmax = self.absmax(f)
             k = int(np.frexp(fmax)[1]) if fmax > 0 else 0
             for it in range(max_iter):
                 self.spectral_solve(r32, out=d32, work=w32)
                 if it == 0:
                     # scale from the first correction (the solution to ~1e-3) and from f:
                     # max |U|, |F| < 2^61
-                    m = max(float(d32.abs().max().item()), fmax)
+                    m = max(self.absmax(d32), fmax)
                     e = 61 - int(np.frexp(m)[1]) if m > 0 else 0
                     _check(self.lib, self.lib.rocketgpu_poisson_to_fx(f.data_ptr(), e, F.data_ptr(), Frem.data_ptr(), n,
                                                                       self._stream()))
@@ -160,8 +171,12 @@ class NeumannPoisson:
                 hist.append(rel)
                 if rel <= tol:
                     break
+            # the solution is fixed up to a constant: the zero-mean one, the mean taken exactly in
+            # fixed point
             u = torch.empty_like(f)
-            _check(self.lib, self.lib.rocketgpu_poisson_fx_to_double(U.data_ptr(), e, u.data_ptr(), n, self._stream()))
+            _check(self.lib, self.lib.rocketgpu_poisson_fx_to_double_zero_mean(U.data_ptr(), e, u.data_ptr(), n,
+                                                                              self._stream()))
+            return u, {"iterations": len(hist), "rel_residual": rel, "history": hist}
         u -= u.mean()  # the solution is fixed up to a constant: return the zero-mean one
         return u, {"iterations": len(hist), "rel_residual": rel, "history": hist}
 

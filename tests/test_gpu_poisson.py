@@ -55,3 +55,45 @@ def test_poisson_fixed_point_floor(rg, cuda):
     assert min(info_fx["history"]) <= 1e-12 and min(info_pr["history"]) <= 1e-12
     d = float(cuda.linalg.vector_norm(u_fx - u_pr) / cuda.linalg.vector_norm(u_pr))
     assert d <= 1e-11, d
+
+
+def test_fixed_point_conversions_bit_exact(rg, cuda):
+    """The integer-arithmetic conversions between float64 and the fixed-point scale: F =
+    round(f 2^e) (half to even) and Frem = float(f - F 2^-e), U 2^-e back to double, and max |x|,
+    each bit-exact against the float64 computation; the zero-mean conversion subtracts the
+    integer mean of U (within one unit of the exact rounding) before scaling."""
+    torch = cuda
+    import ctypes
+
+    P = importlib.import_module("rocket_fft_gb300.poisson")
+    lib = P._bind()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(77)
+    f = rng.standard_normal(200000) * 10.0 ** rng.integers(-8, 4, 200000)
+    f[:8] = [0.0, -0.0, 0.5, 1.5, -2.5, 5e-324, 2.0**-60, 3.0 * 2.0**-62]
+    for e in (0, 20, 52, 58):
+        fe = f[np.abs(np.ldexp(f, e)) < 2.0**62]  # the caller's range: |F| < 2^62
+        fd = torch.from_numpy(fe).cuda()
+        F = torch.empty(fe.size, dtype=torch.int64, device="cuda")
+        Fr = torch.empty(fe.size, dtype=torch.float32, device="cuda")
+        assert lib.rocketgpu_poisson_to_fx(fd.data_ptr(), e, F.data_ptr(), Fr.data_ptr(), fe.size, st) == 0
+        want_F = np.rint(np.ldexp(fe, e)).astype(np.int64)
+        want_r = (fe - np.ldexp(want_F.astype(np.float64), -e)).astype(np.float32)
+        assert np.array_equal(F.cpu().numpy(), want_F), e
+        assert np.array_equal(Fr.cpu().numpy().view(np.uint32), want_r.view(np.uint32)), e
+    U = rng.integers(-2**62, 2**62, 300001, dtype=np.int64)
+    U[:4] = [0, 1, -1, 2**53 + 1]
+    Ud = torch.from_numpy(U).cuda()
+    out = torch.empty(U.size, dtype=torch.float64, device="cuda")
+    for e in (0, 30, 61):
+        assert lib.rocketgpu_poisson_fx_to_double(Ud.data_ptr(), e, out.data_ptr(), U.size, st) == 0
+        assert np.array_equal(out.cpu().numpy(), np.ldexp(U.astype(np.float64), -e)), e
+    e = 40
+    assert lib.rocketgpu_poisson_fx_to_double_zero_mean(Ud.data_ptr(), e, out.data_ptr(), U.size, st) == 0
+    got = out.cpu().numpy()
+    m_exact = round(sum(int(v) for v in U) / U.size)
+    assert any(np.array_equal(got, np.ldexp((U - np.int64(m)).astype(np.float64), -e))
+               for m in (m_exact - 1, m_exact, m_exact + 1))
+    S = P.NeumannPoisson((4, 4, 4))
+    for x in (f, f.astype(np.float32)):
+        assert S.absmax(torch.from_numpy(x).cuda()) == float(np.abs(x).max())
