@@ -162,6 +162,11 @@ int rocketgpu_poisson_fx_to_double_zero_mean(const int64_t *U, int32_t e, double
 /* *out (device double) = max |x| over total float32 (itemsize 4) or float64 (8) elements of a
  * device array, by integer comparison of the bits. */
 int rocketgpu_abs_max(const void *x, int64_t itemsize, int64_t total, double *out, void *stream);
+/* U = round(delta 2^e): the first correction of the fixed-point iterate (no read of U). */
+int rocketgpu_poisson_init_fx(int64_t *U, const float *delta, int64_t total, int32_t e, void *stream);
+/* One pass over the right-hand side f (float64): r32 = float(f) rounded to nearest even,
+ * stats[0] = max |f|, stats[1] = sum of float(f)^2 (device doubles). */
+int rocketgpu_poisson_prepare(const double *f, float *r32, int64_t total, double *stats, void *stream);
 const char *rocketgpu_poisson_last_error(void);
 
 /* ---- batched uneven-length complex FFTs (no reference counterpart) ----

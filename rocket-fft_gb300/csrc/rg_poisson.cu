@@ -167,10 +167,13 @@ __global__ void __launch_bounds__(256) update_kernel(double *uh, float *ul, cons
 // |U| < 2^62, which keeps 2^-e at about 2^-60 of max|u| -- the residual floor this leaves is
 // well below the 1e-12 target.
 
-// U += round(delta * 2^e)
-__global__ void __launch_bounds__(256) fx_update_kernel(long long *U, const float *delta, int64_t total, int e) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
-    U[i] += __float2ll_rn(ldexpf(delta[i], e));
+// U += round(delta * 2^e) (assign: U = round(delta * 2^e), the first correction)
+__global__ void __launch_bounds__(256) fx_update_kernel(long long *U, const float *delta, int64_t total, int e,
+                                                        int assign) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const long long d = __float2ll_rn(ldexpf(delta[i], e));
+    U[i] = assign ? d : U[i] + d;
+  }
 }
 
 // Float of an int64 through the two 32-bit halves of its magnitude (32-bit conversions, no
@@ -381,6 +384,60 @@ __global__ void __launch_bounds__(256) absmax_kernel(const T *x, int64_t total, 
   }
 }
 
+// float(f) rounded to nearest even from the bits of f (no FP64 operation); out of float's
+// normal range the conversion instruction
+__device__ __forceinline__ float float_of(double f) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(f);
+  const int E = int((b >> 52) & 0x7ffull) - 1023 + 127;
+  if (E <= 0 || E >= 254) return __double2float_rn(f);
+  unsigned long long m = (b & 0xfffffffffffffull) >> 29;
+  const unsigned long long rb = b & ((1ull << 29) - 1), half = 1ull << 28;
+  unsigned e = unsigned(E);
+  if (rb > half || (rb == half && (m & 1ull))) {
+    if (++m >> 23) {  // the mantissa carried into the exponent
+      m = 0;
+      ++e;
+    }
+  }
+  return __uint_as_float(unsigned(b >> 63) << 31 | e << 23 | unsigned(m));
+}
+
+// r32 = float(f), stats[0] = max |f| (as the bits of a double, atomic max), stats[1] += sum of
+// float(f)^2 (float per thread, double per CTA): one pass over the right-hand side
+__global__ void __launch_bounds__(256) prepare_kernel(const double *f, float *r32, int64_t total, double *stats) {
+  unsigned long long mx = 0;
+  float ss = 0.f;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const double v = f[i];
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    mx = b > mx ? b : mx;
+    const float x = float_of(v);
+    r32[i] = x;
+    ss = fmaf(x, x, ss);
+  }
+  double ssd = double(ss);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = y > mx ? y : mx;
+    ssd += __shfl_down_sync(0xffffffffu, ssd, o);
+  }
+  __shared__ unsigned long long rm[8];
+  __shared__ double rs[8];
+  if ((threadIdx.x & 31) == 0) {
+    rm[threadIdx.x >> 5] = mx;
+    rs[threadIdx.x >> 5] = ssd;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < int(blockDim.x >> 5); ++w) {
+      mx = rm[w] > mx ? rm[w] : mx;
+      ssd += rs[w];
+    }
+    atomicMax(reinterpret_cast<unsigned long long *>(stats), mx);
+    atomicAdd(stats + 1, ssd);
+  }
+}
+
 thread_local std::string t_err;
 
 template <class F> int guarded(F f) {
@@ -487,7 +544,7 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_update_f
     RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     rg::profiled_launch("poisson_update_fx", uint64_t(total) * 20, st, [&] {
-      fx_update_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<long long *>(U), delta, total, e);
+      fx_update_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<long long *>(U), delta, total, e, 0);
     });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
@@ -552,6 +609,31 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_fx_to_do
     fx_mean_kernel<<<1, 32, 0, st>>>(part, int(g), total, m);
     fx_to_double_kernel<<<g, 256, 0, st>>>(u, out, total, e, m);
     for (int i = 0; i < 3; ++i) rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_init_fx(int64_t *U, const float *delta,
+                                                                               int64_t total, int32_t e,
+                                                                               void *stream) {
+  return guarded([&] {
+    RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    fx_update_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<long long *>(U), delta, total, e, 1);
+    rg::note_launch();
+    RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_prepare(const double *f, float *r32,
+                                                                               int64_t total, double *stats,
+                                                                               void *stream) {
+  return guarded([&] {
+    RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RG_CUDA(cudaMemsetAsync(stats, 0, 2 * sizeof(double), st));
+    prepare_kernel<<<grid_for(total), 256, 0, st>>>(f, r32, total, stats);
+    rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
 }

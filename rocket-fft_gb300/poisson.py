@@ -60,6 +60,10 @@ def _bind():
         lib.rocketgpu_poisson_fx_to_double_zero_mean.restype = ctypes.c_int
         lib.rocketgpu_abs_max.argtypes = [P, i64, i64, P, P]
         lib.rocketgpu_abs_max.restype = ctypes.c_int
+        lib.rocketgpu_poisson_init_fx.argtypes = [P, P, i64, i32, P]
+        lib.rocketgpu_poisson_init_fx.restype = ctypes.c_int
+        lib.rocketgpu_poisson_prepare.argtypes = [P, P, i64, P, P]
+        lib.rocketgpu_poisson_prepare.restype = ctypes.c_int
         lib._poisson_bound = True
     return lib
 
@@ -82,6 +86,7 @@ class NeumannPoisson:
         self.lam32 = self.lam.to(torch.float32)
         self.sumsq = torch.empty(1, dtype=torch.float64, device=self.dev)
         self.amax = torch.empty(1, dtype=torch.float64, device=self.dev)
+        self.stats = torch.empty(2, dtype=torch.float64, device=self.dev)
         self.lib = _bind()
 
     def absmax(self, x):
@@ -122,18 +127,25 @@ class NeumannPoisson:
         assert f.dtype == torch.float64 and f.is_cuda and tuple(f.shape) == self.shape
         assert iterate in ("fixed", "pair")
         f = f.contiguous()
-        fnorm = float(torch.linalg.vector_norm(f).item())
         if not mixed:
+            fnorm = float(torch.linalg.vector_norm(f).item())
             u = self.spectral_solve(f)
             u -= u.mean()
             rel = self.residual(u, f) / fnorm
             return u, {"iterations": 1, "rel_residual": rel, "history": [rel]}
-        r32 = f.to(torch.float32)
+        # float32 copy of f, max |f| and ||f|| in one pass (the norm only normalises the residual:
+        # float squares are plenty)
+        r32 = torch.empty(self.shape, dtype=torch.float32, device=self.dev)
+        _check(self.lib, self.lib.rocketgpu_poisson_prepare(f.data_ptr(), r32.data_ptr(), r32.numel(),
+                                                            self.stats.data_ptr(), self._stream()))
+        fmax_, fss = self.stats.tolist()
+        fnorm = float(np.sqrt(fss))
         d32 = torch.empty_like(r32)
         w32 = torch.empty_like(r32)
         hist = []
         rel = 1.0
         if iterate == "pair":
+            fnorm = float(torch.linalg.vector_norm(f).item())
             u = torch.zeros_like(f)
             u_lo = torch.zeros(self.shape, dtype=torch.float32, device=self.dev)  # iterate = u + u_lo
             for _ in range(max_iter):
@@ -145,12 +157,12 @@ class NeumannPoisson:
                     break
             u += u_lo.double()
         else:
-            U = torch.zeros(self.shape, dtype=torch.int64, device=self.dev)
+            U = torch.empty(self.shape, dtype=torch.int64, device=self.dev)
             F = torch.empty_like(U)
             Frem = torch.empty(self.shape, dtype=torch.float32, device=self.dev)
             e = 0
             n = U.numel()
-            fmax = self.absmax(f)
+            fmax = fmax_
             k = int(np.frexp(fmax)[1]) if fmax > 0 else 0
             for it in range(max_iter):
                 self.spectral_solve(r32, out=d32, work=w32)
@@ -161,8 +173,8 @@ class NeumannPoisson:
                     e = 61 - int(np.frexp(m)[1]) if m > 0 else 0
                     _check(self.lib, self.lib.rocketgpu_poisson_to_fx(f.data_ptr(), e, F.data_ptr(), Frem.data_ptr(), n,
                                                                       self._stream()))
-                _check(self.lib, self.lib.rocketgpu_poisson_update_fx(U.data_ptr(), d32.data_ptr(), n, e,
-                                                                     self._stream()))
+                upd = self.lib.rocketgpu_poisson_init_fx if it == 0 else self.lib.rocketgpu_poisson_update_fx
+                _check(self.lib, upd(U.data_ptr(), d32.data_ptr(), n, e, self._stream()))
                 _check(self.lib, self.lib.rocketgpu_poisson_residual_fx(
                     U.data_ptr(), F.data_ptr(), Frem.data_ptr(), e, k, r32.data_ptr(), *self.shape,
                     self.sumsq.data_ptr(),
