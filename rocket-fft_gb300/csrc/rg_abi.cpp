@@ -6,8 +6,10 @@
 // a thread-local message (rocketgpu_last_status / rocketgpu_last_error).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -191,6 +193,127 @@ void with_views(const Desc &din, const Desc &dout, Body body) {
   }
 }
 
+// ---- host arrays, r2c / c2r over three or more axes: copies overlapped with the passes ----
+//
+// A host call stages its arrays through the GPU, so it is bound by the host link. For r2c the
+// passes over every axis but the outermost only need the planes they work on: the input goes in
+// as slabs of planes on a copy stream, and each slab is transformed as soon as it has arrived;
+// then the outermost axis runs over the whole array and the result goes out. For c2r the
+// outermost axis runs first (in place on the staging copy), then each slab of planes takes the
+// remaining passes and goes out on the copy stream while the next slab is transformed. Dense
+// C-order arrays only, the outermost axis transformed first (axes[0] == 0, three or more axes).
+
+cudaStream_t copy_stream() {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (!streams[dev]) RG_CUDA(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
+  return streams[dev];
+}
+
+bool dense_c(const Desc &d) {
+  int64_t acc = d.itemsize;
+  for (int i = int(d.shape.size()) - 1; i >= 0; --i) {
+    if (d.shape[i] != 1 && d.bstride[i] != acc) return false;
+    acc *= d.shape[i];
+  }
+  return true;
+}
+
+NdArray dense_view(void *data, std::vector<int64_t> shape) {
+  NdArray v;
+  v.data = data;
+  v.shape = std::move(shape);
+  v.stride.assign(v.shape.size(), 1);
+  for (int i = int(v.shape.size()) - 2; i >= 0; --i) v.stride[i] = v.stride[i + 1] * v.shape[i + 1];
+  return v;
+}
+
+bool pipeline_ok(const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax) {
+  if (ax.size() < 3 || ax[0] != 0 || din.shape.empty() || din.shape[0] < 2) return false;
+  for (size_t i = 1; i < ax.size(); ++i)
+    if (ax[i] == 0) return false;
+  if (!dense_c(din) || !dense_c(dout) || !din.data || !dout.data) return false;
+  return !is_device_ptr(din.data) && !is_device_ptr(dout.data);
+}
+
+// r2c (forward, fct) of host din into host dout, pipelined as described above.
+void pipelined_r2c(DType dt, const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax, bool forward,
+                   double fct) {
+  cudaStream_t st = t_stream, cs = copy_stream();
+  const int64_t n0 = din.shape[0];
+  const int64_t plane_in = din.bstride[0], plane_out = dout.bstride[0];
+  rg::DevBuf bin(size_t(n0 * plane_in), st), bout(size_t(n0 * plane_out), st);
+  cudaEvent_t ready;
+  RG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  RG_CUDA(cudaEventRecord(ready, st));  // the buffers exist in st's order
+  RG_CUDA(cudaStreamWaitEvent(cs, ready, 0));
+  const int64_t K = std::min<int64_t>(4, n0), per = (n0 + K - 1) / K;
+  std::vector<cudaEvent_t> arrived;
+  const rg::Axes rest(ax.begin() + 1, ax.end());
+  for (int64_t c0 = 0; c0 < n0; c0 += per) {
+    const int64_t cn = std::min(per, n0 - c0);
+    cudaEvent_t ev;
+    RG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(bin.get()) + c0 * plane_in,
+                            static_cast<const char *>(din.data) + c0 * plane_in, size_t(cn * plane_in),
+                            cudaMemcpyHostToDevice, cs));
+    RG_CUDA(cudaEventRecord(ev, cs));
+    arrived.push_back(ev);
+    RG_CUDA(cudaStreamWaitEvent(st, ev, 0));
+    std::vector<int64_t> si = din.shape, so = dout.shape;
+    si[0] = so[0] = cn;
+    rg::exec_r2c(dt, dense_view(static_cast<char *>(bin.get()) + c0 * plane_in, si),
+                 dense_view(static_cast<char *>(bout.get()) + c0 * plane_out, so), rest, forward, fct, st);
+  }
+  const NdArray whole = dense_view(bout.get(), dout.shape);
+  rg::exec_c2c(dt, whole, whole, rg::Axes{0}, forward, 1.0, st);
+  RG_CUDA(cudaMemcpyAsync(dout.data, bout.get(), size_t(n0 * plane_out), cudaMemcpyDeviceToHost, st));
+  RG_CUDA(cudaStreamSynchronize(st));
+  for (cudaEvent_t e : arrived) cudaEventDestroy(e);
+  cudaEventDestroy(ready);
+}
+
+// c2r (forward, fct) of host din into host dout, pipelined as described above.
+void pipelined_c2r(DType dt, const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax, bool forward,
+                   double fct) {
+  cudaStream_t st = t_stream, cs = copy_stream();
+  const int64_t n0 = dout.shape[0];
+  const int64_t plane_in = din.bstride[0], plane_out = dout.bstride[0];
+  rg::DevBuf bin(size_t(n0 * plane_in), st), bout(size_t(n0 * plane_out), st);
+  RG_CUDA(cudaMemcpyAsync(bin.get(), din.data, size_t(n0 * plane_in), cudaMemcpyHostToDevice, st));
+  const NdArray whole = dense_view(bin.get(), din.shape);
+  rg::exec_c2c(dt, whole, whole, rg::Axes{0}, forward, 1.0, st);  // in place on the staging copy
+  const int64_t K = std::min<int64_t>(4, n0), per = (n0 + K - 1) / K;
+  const rg::Axes rest(ax.begin() + 1, ax.end());
+  std::vector<cudaEvent_t> done;
+  for (int64_t c0 = 0; c0 < n0; c0 += per) {
+    const int64_t cn = std::min(per, n0 - c0);
+    std::vector<int64_t> si = din.shape, so = dout.shape;
+    si[0] = so[0] = cn;
+    rg::exec_c2r(dt, dense_view(static_cast<char *>(bin.get()) + c0 * plane_in, si),
+                 dense_view(static_cast<char *>(bout.get()) + c0 * plane_out, so), rest, forward, fct, st);
+    cudaEvent_t ev;
+    RG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    RG_CUDA(cudaEventRecord(ev, st));
+    done.push_back(ev);
+    RG_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(dout.data) + c0 * plane_out,
+                            static_cast<char *>(bout.get()) + c0 * plane_out, size_t(cn * plane_out),
+                            cudaMemcpyDeviceToHost, cs));
+  }
+  RG_CUDA(cudaStreamSynchronize(cs));
+  // the buffers go back to the pool in st's order once the copies on cs are done
+  cudaEvent_t fin;
+  RG_CUDA(cudaEventCreateWithFlags(&fin, cudaEventDisableTiming));
+  RG_CUDA(cudaEventRecord(fin, cs));
+  RG_CUDA(cudaStreamWaitEvent(st, fin, 0));
+  for (cudaEvent_t e : done) cudaEventDestroy(e);
+  cudaEventDestroy(fin);
+}
+
 void check_same_shape(const Desc &a, const Desc &b) {
   RG_CHECK(a.shape == b.shape, RG_ERR_ARG, "input and output shapes differ");
 }
@@ -242,6 +365,10 @@ int do_r2c(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_
     else
       check_half_shape(din, dout, ax);
     if (any_zero(din.shape)) return;
+    if (!sym && bscale == 1.0 && pipeline_ok(din, dout, ax)) {
+      pipelined_r2c(dt, din, dout, ax, forward, fct);
+      return;
+    }
     with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
       if (sym)
         rg::exec_c2c_sym(dt, i, o, ax, forward, fct, st);
@@ -261,6 +388,10 @@ int do_c2r(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_
     RG_CHECK(!ax.empty(), RG_ERR_ARG, "at least one axis is required");
     check_half_shape(dout, din, ax);
     if (any_zero(dout.shape)) return;
+    if (bscale == 1.0 && pipeline_ok(din, dout, ax)) {
+      pipelined_c2r(dt, din, dout, ax, forward, fct);
+      return;
+    }
     with_views(din, dout, [&](const NdArray &i, const NdArray &o, cudaStream_t st) {
       rg::exec_c2r(dt, i, o, ax, forward, fct, st, bscale);
     });

@@ -136,3 +136,27 @@ def test_c2c_large_lengths(rg, cuda, cdt):
         rg.c2c(xd, X, ax, True, 1.0, 1)
         e = oracle.rel_l2(X.cpu().numpy(), want)
         assert e <= TOL[np.dtype(cdt)], (n, e)
+
+
+@pytest.mark.parametrize("shape,axes", [((256, 256, 256), (0, 1, 2)), ((7, 32, 34), (0, 1, 2)),
+                                        ((10, 12, 40), (0, 2, 1)), ((5, 3, 16, 18), (0, 1, 2, 3))])
+def test_host_r2c_c2r_pipelined(rg, cuda, shape, axes):
+    """r2c / c2r of host (NumPy) arrays over three or more axes, outermost first: the library
+    overlaps the slab copies with the passes that do not need the whole array. Same results as
+    the oracle (float32: relative L2 <= 1e-6)."""
+    rng = np.random.default_rng(44)
+    P = oracle.port()
+    x = rng.standard_normal(shape).astype(np.float32)
+    hshape = list(shape)
+    hshape[axes[-1]] = shape[axes[-1]] // 2 + 1
+    X = np.empty(hshape, np.complex64)
+    rg.r2c(x, X, np.array(axes, np.int64), True, 1.0, 1)
+    want = np.empty(hshape, np.complex128)
+    P.r2c(x.astype(np.float64), want, list(axes), True, 1.0, 8)
+    assert oracle.rel_l2(X, want) <= TOL[np.dtype(np.complex64)]
+    n = int(np.prod([shape[a] for a in axes]))
+    y = np.empty(shape, np.float32)
+    rg.c2r(X, y, np.array(axes, np.int64), False, 1.0 / n, 1)
+    want_y = np.empty(shape, np.float64)
+    P.c2r(X.astype(np.complex128), want_y, list(axes), False, 1.0 / n, 8)
+    assert oracle.rel_l2(y, want_y) <= TOL[np.dtype(np.float32)]
