@@ -121,6 +121,21 @@ def dist_init():
     return world, rank, local
 
 
+def max_over_ranks(torch, value, world, device):
+    """The largest of every rank's `value` (the job's time is its slowest rank's); `value`
+    itself for a single process. Collective on the default process group."""
+    if world <= 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_step, steps, ms):
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return world * units_per_step * steps / (ms / 1e3)
+
+
 def timed_steps(torch, step, steps, warmup, local, world):
     """Run `warmup` untimed steps, then time exactly `steps` steps on the current stream with
     CUDA events between barriers, sampling clocks meanwhile. Returns (ms, clocks, launches)."""
@@ -142,11 +157,7 @@ def timed_steps(torch, step, steps, warmup, local, world):
             step(i)
         stop.record(stream)
         torch.cuda.synchronize()
-    ms = start.elapsed_time(stop)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, start.elapsed_time(stop), world, "cuda")
     return ms, clk.summary(), rg.launch_count() - launches0
 
 
@@ -215,7 +226,7 @@ def run_c1(args):
         rg.c2c(xs[i % rot], ys[i % rot], axes, True, 1.0, 1)
 
     ms, clocks, launches = timed_steps(torch, step, args.steps, args.warmup, local, world)
-    value = world * 256 * args.steps / (ms / 1e3)
+    value = job_rate(world, 256, args.steps, ms)
     kernels, roof = kernel_profile(step, args.steps)
     x0 = xs[0].cpu().numpy()
     step(0)
@@ -278,7 +289,7 @@ def run_c4(args):
         loss.backward()
 
     ms, clocks, launches = timed_steps(torch, step, args.steps, args.warmup, local, world)
-    value = world * 128 * args.steps / (ms / 1e3)  # 64 forward + 64 adjoint transforms per step
+    value = job_rate(world, 128, args.steps, ms)  # 64 forward + 64 adjoint transforms per step
     kernels, roof = kernel_profile(step, args.steps)
     # gradient check against torch.fft autograd on one 1024^2 slice (CPU, float64)
     x0 = xs[0].detach()[:1].double().cpu().requires_grad_(True)
@@ -360,7 +371,7 @@ def run_c5(args):
            "unit": "solves/s", "h2d_bytes_per_step": fh.numel() * 8, "d2h_bytes_per_step": uh.numel() * 8,
            "path": "poisson.NeumannPoisson.solve on a pinned host right-hand side copied in, solution copied out"}
     a = argparse.Namespace(steps=steps, warmup=min(args.warmup, 3))
-    line = base_line("solves/s", world * steps / (ms / 1e3), "solves/s", world, a, ms, "f32 transforms + f64 refinement",
+    line = base_line("solves/s", job_rate(world, 1, steps, ms), "solves/s", world, a, ms, "f32 transforms + f64 refinement",
                      {"workload": "Neumann Poisson, 512^3 float64 RHS = 64 Gaussian blobs (zero mean), "
                                   "dctn II -> eigen-divide -> dctn III, refinement to 1e-12",
                       "global_batch": world, "l2": "1 GiB arrays > L2"})
@@ -404,7 +415,7 @@ def run_c3(args):
 
     ms, clocks, _ = timed_steps(torch, step, args.steps, args.warmup, local, world)
     launches = args.steps  # one persistent kernel per replayed graph (the library cannot count replays)
-    value = world * len(lengths) * args.steps / (ms / 1e3)
+    value = job_rate(world, len(lengths), args.steps, ms)
     bytes_step = 2 * plan.total * 8
     peak, peak_kind = peaks()
     achieved = bytes_step / (ms / args.steps / 1e3) / 1e9
@@ -568,12 +579,8 @@ def run_ours(args):
         stop.record(stream)
         barrier()
     launches = rg.launch_count() - launches0
-    ms = start.elapsed_time(stop)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 2 * args.steps / (ms / 1e3)
+    ms = max_over_ranks(torch, start.elapsed_time(stop), world, dev)
+    value = job_rate(world, 2, args.steps, ms)
 
     # accuracy of one step against the FP64 oracle (host, this rank's first volume)
     acc = {}
