@@ -177,6 +177,35 @@ def e2e_rate(torch, steps, h2d, run, d2h, units):
     return units * steps / (time.perf_counter() - t0)
 
 
+def host_link_floor(torch, h_in, h_out, dev, h2d_bytes, d2h_bytes, ms_per_step, reps=5):
+    """The host link's own rates, measured here with plain copies of the workload's arrays
+    (pinned host <-> device, CUDA events, median of `reps`), and the time a step's copies take
+    at those rates when they run one after another. A round trip through host arrays is a chain
+    (each transform's output depends on all of its input, and the inverse reads the forward's
+    result), so that time is the floor of the e2e step; `frac` = floor / measured step."""
+    stream = torch.cuda.current_stream()
+
+    def median_ms(fn):
+        out = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            out.append(a.elapsed_time(b))
+        return sorted(out)[len(out) // 2]
+
+    flat_in, flat_out, flat_dev = h_in.view(-1), h_out.view(-1), dev.view(-1)
+    t_h2d = median_ms(lambda: flat_dev.copy_(flat_in, non_blocking=True))
+    t_d2h = median_ms(lambda: flat_out.copy_(flat_dev, non_blocking=True))
+    h2d_gbs = flat_in.numel() * flat_in.element_size() / (t_h2d / 1e3) / 1e9
+    d2h_gbs = flat_out.numel() * flat_out.element_size() / (t_d2h / 1e3) / 1e9
+    floor_ms = 1e3 * (h2d_bytes / (h2d_gbs * 1e9) + d2h_bytes / (d2h_gbs * 1e9))
+    return {"h2d_gbs": h2d_gbs, "d2h_gbs": d2h_gbs, "floor_ms_per_step": floor_ms,
+            "ms_per_step": ms_per_step, "frac": floor_ms / ms_per_step}
+
+
 def kernel_profile(step, steps):
     """Per-kernel device time and algorithmic bytes over `steps` steps (events around every
     launch of the library); returns (stats, roofline dict of the dominant kernel)."""
@@ -663,9 +692,11 @@ def run_ours(args):
             rg.r2c(nx, nX, AXES, True, 1.0, 1)
             rg.c2r(nX, ny, AXES, False, FCT_INV, 1)
         dt = time.perf_counter() - t0
+        h2d_b, d2h_b = int(nx.nbytes + nX.nbytes), int(nX.nbytes + ny.nbytes)
         e2e = {"value": 2 * args.steps / dt, "unit": "transforms/s",
-               "h2d_bytes_per_step": int(nx.nbytes + nX.nbytes), "d2h_bytes_per_step": int(nX.nbytes + ny.nbytes),
-               "path": "numba_r2c/numba_c2r C ABI, host pinned numpy arrays staged by the library"}
+               "h2d_bytes_per_step": h2d_b, "d2h_bytes_per_step": d2h_b,
+               "path": "numba_r2c/numba_c2r C ABI, host pinned numpy arrays staged by the library",
+               "link": host_link_floor(torch, hx, hy, xs[0], h2d_b, d2h_b, 1e3 * dt / args.steps)}
 
     # CPU baseline: bounded sample of the same workload on the host (rank 0 only)
     cpu = None

@@ -10,11 +10,14 @@
 // (good_size, largest_prime_factor, cost_guess), the packed-vs-Bluestein decision, the
 // Bluestein construction, the FFTPACK half-complex layout, the DCT/DST reductions, fct
 // placement, the N-d axis loop and the Hermitian fills of c2c_sym / genuine Hartley.
-// What differs: the complex radix passes are a Stockham formulation (radix 4, 2, 3, 5 and a
-// generic odd radix) instead of FFTPACK's pass2..pass11/passg, and the real transform is a
-// half-length complex FFT plus a split instead of rfftp's radf/radb passes. Those produce
-// the same transforms up to rounding.
+// What differs: the complex radix passes are a Stockham formulation (radix 8, 4, 2, 3, 5 and a
+// generic odd radix, in cfftp's factor order) instead of FFTPACK's pass2..pass11/passg, and the
+// real transform is a half-length complex FFT plus a split instead of rfftp's radf/radb passes.
+// Those produce the same transforms up to rounding. Rows run several at a time in 16-byte lane
+// vectors, as the reference's SIMD path does, so the port is also a fair CPU timing baseline.
 #include <algorithm>
+#include <condition_variable>
+#include <functional>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -24,7 +27,10 @@
 #include <stdexcept>
 #include <thread>
 #include <tuple>
+#include <type_traits>
 #include <vector>
+
+#include <unistd.h>
 
 namespace port {
 
@@ -34,13 +40,72 @@ using i64 = int64_t;
 template <class T> struct C {
   T r, i;
 };
-template <class T> inline C<T> operator+(C<T> a, C<T> b) { return {a.r + b.r, a.i + b.i}; }
-template <class T> inline C<T> operator-(C<T> a, C<T> b) { return {a.r - b.r, a.i - b.i}; }
+// Complex numbers of scalars (plan tables) or of lane vectors (the data of several rows at
+// once); the operators below are generic over both.
+template <class D> inline C<D> operator+(C<D> a, C<D> b) { return {a.r + b.r, a.i + b.i}; }
+template <class D> inline C<D> operator-(C<D> a, C<D> b) { return {a.r - b.r, a.i - b.i}; }
 template <class T> inline C<T> operator*(C<T> a, C<T> b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
 template <class T> inline C<T> operator*(C<T> a, T s) { return {a.r * s, a.i * s}; }
-template <class T> inline C<T> conj(C<T> a) { return {a.r, -a.i}; }
-// multiply by conj(b) when `cj`
-template <class T> inline C<T> mulx(C<T> a, C<T> b, bool cj) { return cj ? a * conj(b) : a * b; }
+template <class D> inline C<D> conj(C<D> a) { return {a.r, -a.i}; }
+// data times a real scalar
+template <class D, class S> inline C<D> scale(C<D> a, S s) { return {a.r * s, a.i * s}; }
+// data times a table entry w, or times conj(w) when CJ
+template <bool CJ, class D, class T> inline C<D> tmul(C<D> a, C<T> w) {
+  if constexpr (CJ)
+    return {a.r * w.r + a.i * w.i, a.i * w.r - a.r * w.i};
+  else
+    return {a.r * w.r - a.i * w.i, a.r * w.i + a.i * w.r};
+}
+
+// Scratch array of n elements from a per-thread pool that is kept across calls, as the
+// reference keeps one temporary per thread for all rows (HDR:3471-3494): one pool per call site
+// (`slot`), so that nested users never share one; 64-byte aligned, contents undefined (every
+// element is written before it is read). Reusing the memory matters beyond the allocation
+// cost: a fresh block per row group made power-of-two strided gathers 2x slower.
+enum Slot { kRows = 0, kRealZ, kRealX, kPass, kBlue, kDcst, kGenV, kGenS, kGenD, kSlots };
+template <class X> class Scratch {
+ public:
+  Scratch(size_t n, Slot slot) {
+    thread_local std::vector<char> pools[kSlots];
+    std::vector<char> &p = pools[slot];
+    const size_t need = n * sizeof(X) + 64;
+    if (p.size() < need) p.resize(need);
+    p_ = reinterpret_cast<X *>((reinterpret_cast<uintptr_t>(p.data()) + 63) & ~uintptr_t(63));
+  }
+  X &operator[](size_t i) { return p_[i]; }
+  const X &operator[](size_t i) const { return p_[i]; }
+  X *data() { return p_; }
+
+ private:
+  X *p_;
+};
+
+// Rows are transformed W at a time in 16-byte lane vectors (GCC vector extensions: SSE2 on
+// x86-64, NEON on AArch64, no -march needed), as the reference's multi-row SIMD path does
+// (HDR:3455-3470, 3585-3595); leftover rows go through the same code with W = 1.
+template <class T> struct VecOf;
+template <> struct VecOf<float> { using type = float __attribute__((vector_size(16))); };
+template <> struct VecOf<double> { using type = double __attribute__((vector_size(16))); };
+template <class T> constexpr int kLanes = int(16 / sizeof(T));
+template <class T, int W> struct Lanes {
+  using D = std::conditional_t<W == 1, T, typename VecOf<T>::type>;
+  static T get(const D &v, int l) {
+    if constexpr (W == 1) {
+      (void)l;
+      return v;
+    } else {
+      return v[l];
+    }
+  }
+  static void set(D &v, int l, T x) {
+    if constexpr (W == 1) {
+      (void)l;
+      v = x;
+    } else {
+      v[l] = x;
+    }
+  }
+};
 
 // ---------------------------------------------------------------------------------------
 // size utilities (HDR:546-650)
@@ -127,14 +192,20 @@ template <class T> class CPack {
  public:
   explicit CPack(u64 n) : n_(n) {
     if (n == 0) throw std::runtime_error("zero-length FFT requested");
+    // factor order of cfftp::factorize (HDR:1750-1778): 8s, 4s, one 2 moved to the front, odd
     u64 len = n;
+    while (len % 8 == 0) {
+      fac_.push_back(8);
+      len /= 8;
+    }
     while (len % 4 == 0) {
       fac_.push_back(4);
       len /= 4;
     }
     if (len % 2 == 0) {
-      fac_.insert(fac_.begin(), 2);
       len /= 2;
+      fac_.push_back(2);
+      std::swap(fac_.front(), fac_.back());
     }
     for (u64 d = 3; d * d <= len; d += 2)
       while (len % d == 0) {
@@ -147,7 +218,7 @@ template <class T> class CPack {
       off_.push_back(tw_.size());
       for (u64 k = 1; k < R; ++k)
         for (u64 m = 0; m < ns; ++m) tw_.push_back(unit<T>(m * k, ns * R));  // e^{+}
-      if (R > 5) {
+      if (generic(R)) {
         roots_off_.push_back(rt_.size());
         for (u64 t = 0; t < R; ++t) rt_.push_back(unit<T>(t, R));
       } else {
@@ -159,99 +230,162 @@ template <class T> class CPack {
   u64 length() const { return n_; }
 
   // forward: exponent -2 pi i (pocketfft's fwd=true); scale by fct at the end
-  void exec(C<T> *c, T fct, bool fwd) const {
+  template <class D> void exec(C<D> *c, T fct, bool fwd) const { fwd ? run<true>(c, fct) : run<false>(c, fct); }
+
+ private:
+  static bool generic(u64 R) { return R != 2 && R != 3 && R != 4 && R != 5 && R != 8; }
+
+  template <bool FWD, class D> void run(C<D> *c, T fct) const {
     if (n_ == 1) {
-      c[0] = c[0] * fct;
+      c[0] = scale(c[0], fct);
       return;
     }
-    std::vector<C<T>> buf(n_);
-    C<T> *a = c, *b = buf.data();
+    // out of place passes: c -> s1, then s1 <-> s2, the last one back into c (two or more passes)
+    const size_t np = fac_.size();
+    Scratch<C<D>> buf((np > 2 ? 2 : 1) * n_, kPass);
+    C<D> *s1 = buf.data(), *s2 = np > 2 ? s1 + n_ : nullptr;
+    const C<D> *a = c;
     u64 ns = 1;
-    for (size_t p = 0; p < fac_.size(); ++p) {
-      pass(fac_[p], ns, a, b, tw_.data() + off_[p], rt_.data() + roots_off_[p], fwd);
-      std::swap(a, b);
-      ns *= fac_[p];
+    for (size_t p = 0; p < np; ++p) {
+      C<D> *b = p + 1 == np && np > 1 ? c : (p % 2 == 0 ? s1 : s2);
+      const u64 R = fac_[p];
+      const C<T> *tw = tw_.data() + off_[p];
+      switch (R) {
+        case 2: pass<FWD, 2>(ns, a, b, tw, [](C<D>(&v)[2]) { dft2(v); }); break;
+        case 3: pass<FWD, 3>(ns, a, b, tw, [](C<D>(&v)[3]) { dft3<FWD>(v); }); break;
+        case 4: pass<FWD, 4>(ns, a, b, tw, [](C<D>(&v)[4]) { dft4<FWD>(v); }); break;
+        case 5: pass<FWD, 5>(ns, a, b, tw, [](C<D>(&v)[5]) { dft5<FWD>(v); }); break;
+        case 8: pass<FWD, 8>(ns, a, b, tw, [](C<D>(&v)[8]) { dft8<FWD>(v); }); break;
+        default: passg<FWD>(R, ns, a, b, tw, rt_.data() + roots_off_[p]);
+      }
+      a = b;
+      ns *= R;
     }
-    if (a != c) {
-      for (u64 i = 0; i < n_; ++i) c[i] = a[i] * fct;
+    if (a != c) {  // a single pass
+      for (u64 i = 0; i < n_; ++i) c[i] = scale(a[i], fct);
     } else if (fct != T(1)) {
-      for (u64 i = 0; i < n_; ++i) c[i] = c[i] * fct;
+      for (u64 i = 0; i < n_; ++i) c[i] = scale(c[i], fct);
     }
   }
 
- private:
-  void pass(u64 R, u64 ns, const C<T> *x, C<T> *y, const C<T> *tw, const C<T> *rt, bool fwd) const {
+  // One Stockham pass of radix R: butterfly (b0, m) reads x[j + k L] (j = b0 + m), twiddles
+  // input k by (conj when forward) e^{+2 pi i m k / (ns R)}, writes y[b0 R + m + q ns].
+  template <bool FWD, int R, class D, class Bfly>
+  void pass(u64 ns, const C<D> *__restrict__ x, C<D> *__restrict__ y, const C<T> *__restrict__ tw, Bfly bfly) const {
     const u64 L = n_ / R;
-    const bool cj = fwd;  // forward uses conj(e^{+}) = e^{-}
-    C<T> v[64];
-    std::vector<C<T>> vb;
-    C<T> *vv = v;
-    if (R > 64) {
-      vb.resize(2 * R);
-      vv = vb.data();
-    }
     for (u64 b0 = 0; b0 < L; b0 += ns) {
       for (u64 m = 0; m < ns; ++m) {
         const u64 j = b0 + m;
-        for (u64 k = 0; k < R; ++k) vv[k] = x[j + k * L];
+        C<D> v[R];
+        for (int k = 0; k < R; ++k) v[k] = x[j + k * L];
         if (ns > 1)
-          for (u64 k = 1; k < R; ++k) vv[k] = mulx(vv[k], tw[(k - 1) * ns + m], cj);
-        C<T> *out = y + b0 * R + m;
-        switch (R) {
-          case 2: {
-            out[0] = vv[0] + vv[1];
-            out[ns] = vv[0] - vv[1];
-            break;
+          for (int k = 1; k < R; ++k) v[k] = tmul<FWD>(v[k], tw[(k - 1) * ns + m]);
+        bfly(v);
+        C<D> *out = y + b0 * R + m;
+        for (int q = 0; q < R; ++q) out[q * ns] = v[q];
+      }
+    }
+  }
+
+  // generic odd radix R: with s_k = v_k + v_{R-k}, d_k = v_k - v_{R-k} (k = 1..(R-1)/2) and
+  // theta = 2 pi q k / R, y_q = A_q -+ i B_q and y_{R-q} = A_q +- i B_q (upper signs forward),
+  // A_q = v_0 + sum_k s_k cos theta, B_q = sum_k d_k sin theta; y_0 = v_0 + sum_k s_k
+  template <bool FWD, class D>
+  void passg(u64 R, u64 ns, const C<D> *x, C<D> *y, const C<T> *tw, const C<T> *rt) const {
+    const u64 L = n_ / R, H = (R - 1) / 2;
+    Scratch<C<D>> v(R, kGenV), sk(H + 1, kGenS), dk(H + 1, kGenD);
+    for (u64 b0 = 0; b0 < L; b0 += ns) {
+      for (u64 m = 0; m < ns; ++m) {
+        const u64 j = b0 + m;
+        for (u64 k = 0; k < R; ++k) v[k] = x[j + k * L];
+        if (ns > 1)
+          for (u64 k = 1; k < R; ++k) v[k] = tmul<FWD>(v[k], tw[(k - 1) * ns + m]);
+        C<D> y0 = v[0];
+        for (u64 k = 1; k <= H; ++k) {
+          sk[k] = v[k] + v[R - k];
+          dk[k] = v[k] - v[R - k];
+          y0 = y0 + sk[k];
+        }
+        C<D> *out = y + b0 * R + m;
+        out[0] = y0;
+        for (u64 q = 1; q <= H; ++q) {
+          C<D> A = v[0], B = {D{}, D{}};
+          u64 e = 0;
+          for (u64 k = 1; k <= H; ++k) {
+            e += q;
+            if (e >= R) e -= R;
+            A = A + scale(sk[k], rt[e].r);
+            B = B + scale(dk[k], rt[e].i);
           }
-          case 4: {
-            const C<T> t0 = vv[0] + vv[2], t1 = vv[0] - vv[2], t2 = vv[1] + vv[3];
-            C<T> t3 = vv[1] - vv[3];
-            t3 = fwd ? C<T>{t3.i, -t3.r} : C<T>{-t3.i, t3.r};  // * (-i) or * (+i)
-            out[0] = t0 + t2;
-            out[2 * ns] = t0 - t2;
-            out[ns] = t1 + t3;
-            out[3 * ns] = t1 - t3;
-            break;
-          }
-          case 3: {
-            const T c1 = T(-0.5), s1 = T(fwd ? -0.86602540378443864676 : 0.86602540378443864676);
-            const C<T> s = vv[1] + vv[2], d = vv[1] - vv[2];
-            const C<T> a = vv[0] + s * c1;
-            const C<T> b = {-d.i * s1, d.r * s1};  // i * s1 * d
-            out[0] = vv[0] + s;
-            out[ns] = a + b;
-            out[2 * ns] = a - b;
-            break;
-          }
-          case 5: {
-            const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);
-            const T sg = fwd ? T(-1) : T(1);
-            const T s1 = sg * T(0.95105651629515357212), s2 = sg * T(0.58778525229247312917);
-            const C<T> sa = vv[1] + vv[4], da = vv[1] - vv[4], sb = vv[2] + vv[3], db = vv[2] - vv[3];
-            const C<T> a1 = vv[0] + sa * c1 + sb * c2, a2 = vv[0] + sa * c2 + sb * c1;
-            const C<T> e1 = da * s1 + db * s2, e2 = da * s2 - db * s1;
-            const C<T> b1 = {-e1.i, e1.r}, b2 = {-e2.i, e2.r};
-            out[0] = vv[0] + sa + sb;
-            out[ns] = a1 + b1;
-            out[4 * ns] = a1 - b1;
-            out[2 * ns] = a2 + b2;
-            out[3 * ns] = a2 - b2;
-            break;
-          }
-          default: {  // generic radix: y_q = sum_k v_k w^{qk}
-            for (u64 q = 0; q < R; ++q) {
-              C<T> acc = vv[0];
-              u64 e = 0;
-              for (u64 k = 1; k < R; ++k) {
-                e += q;
-                if (e >= R) e -= R;
-                acc = acc + mulx(vv[k], rt[e], cj);
-              }
-              out[q * ns] = acc;
-            }
-          }
+          const C<D> iB = {-B.i, B.r};  // i B
+          out[q * ns] = FWD ? A - iB : A + iB;
+          out[(R - q) * ns] = FWD ? A + iB : A - iB;
         }
       }
+    }
+  }
+
+  // multiply by -i (forward) or +i (backward)
+  template <bool FWD, class D> static C<D> rot90(C<D> a) {
+    if constexpr (FWD)
+      return {a.i, -a.r};
+    else
+      return {-a.i, a.r};
+  }
+  template <class D> static void dft2(C<D> (&v)[2]) {
+    const C<D> a = v[0];
+    v[0] = a + v[1];
+    v[1] = a - v[1];
+  }
+  template <bool FWD, class D> static void dft3(C<D> (&v)[3]) {
+    const T c1 = T(-0.5), s1 = T(FWD ? -0.86602540378443864676 : 0.86602540378443864676);
+    const C<D> s = v[1] + v[2], d = v[1] - v[2];
+    const C<D> a = v[0] + scale(s, c1);
+    const C<D> b = {-d.i * s1, d.r * s1};  // i * s1 * d
+    v[0] = v[0] + s;
+    v[1] = a + b;
+    v[2] = a - b;
+  }
+  template <bool FWD, class D> static void dft4(C<D> (&v)[4]) {
+    const C<D> t0 = v[0] + v[2], t1 = v[0] - v[2], t2 = v[1] + v[3];
+    const C<D> t3 = rot90<FWD>(v[1] - v[3]);
+    v[0] = t0 + t2;
+    v[2] = t0 - t2;
+    v[1] = t1 + t3;
+    v[3] = t1 - t3;
+  }
+  template <bool FWD, class D> static void dft5(C<D> (&v)[5]) {
+    const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);
+    const T sg = FWD ? T(-1) : T(1);
+    const T s1 = sg * T(0.95105651629515357212), s2 = sg * T(0.58778525229247312917);
+    const C<D> sa = v[1] + v[4], da = v[1] - v[4], sb = v[2] + v[3], db = v[2] - v[3];
+    const C<D> a1 = v[0] + scale(sa, c1) + scale(sb, c2), a2 = v[0] + scale(sa, c2) + scale(sb, c1);
+    const C<D> e1 = scale(da, s1) + scale(db, s2), e2 = scale(da, s2) - scale(db, s1);
+    const C<D> b1 = {-e1.i, e1.r}, b2 = {-e2.i, e2.r};
+    v[0] = v[0] + sa + sb;
+    v[1] = a1 + b1;
+    v[4] = a1 - b1;
+    v[2] = a2 + b2;
+    v[3] = a2 - b2;
+  }
+  // radix 8 as two radix-4 transforms (even / odd inputs) and the eighth-root rotations
+  template <bool FWD, class D> static void dft8(C<D> (&v)[8]) {
+    C<D> a[4] = {v[0], v[2], v[4], v[6]}, b[4] = {v[1], v[3], v[5], v[7]};
+    dft4<FWD>(a);
+    dft4<FWD>(b);
+    const T h = T(0.70710678118654752440084436210484904);
+    const C<D> x1 = b[1], x3 = b[3];
+    if constexpr (FWD) {  // b_q *= e^{-2 pi i q / 8}
+      b[1] = {(x1.r + x1.i) * h, (x1.i - x1.r) * h};
+      b[3] = {(x3.i - x3.r) * h, -(x3.r + x3.i) * h};
+    } else {  // b_q *= e^{+2 pi i q / 8}
+      b[1] = {(x1.r - x1.i) * h, (x1.r + x1.i) * h};
+      b[3] = {-(x3.r + x3.i) * h, (x3.r - x3.i) * h};
+    }
+    b[2] = rot90<FWD>(b[2]);
+    for (int q = 0; q < 4; ++q) {
+      v[q] = a[q] + b[q];
+      v[q + 4] = a[q] - b[q];
     }
   }
 
@@ -286,16 +420,19 @@ template <class T> class Blue {
   }
   u64 length() const { return n_; }
 
-  void exec(C<T> *c, T fct, bool fwd) const {  // HDR:2732-2762
-    std::vector<C<T>> a(n2_, C<T>{T(0), T(0)});
-    for (u64 m = 0; m < n_; ++m) a[m] = mulx(c[m], bk_[m], fwd);
-    plan_.exec(a.data(), T(1), true);
-    for (u64 m = 0; m < n2_; ++m) a[m] = mulx(a[m], bkf_[m], !fwd);
-    plan_.exec(a.data(), T(1), false);
-    for (u64 m = 0; m < n_; ++m) c[m] = mulx(a[m], bk_[m], fwd) * fct;
-  }
+  template <class D> void exec(C<D> *c, T fct, bool fwd) const { fwd ? run<true>(c, fct) : run<false>(c, fct); }
 
  private:
+  template <bool FWD, class D> void run(C<D> *c, T fct) const {  // HDR:2732-2762
+    Scratch<C<D>> a(n2_, kBlue);
+    std::fill(a.data() + n_, a.data() + n2_, C<D>{D{}, D{}});  // zero padding
+    for (u64 m = 0; m < n_; ++m) a[m] = tmul<FWD>(c[m], bk_[m]);
+    plan_.exec(a.data(), T(1), true);
+    for (u64 m = 0; m < n2_; ++m) a[m] = tmul<!FWD>(a[m], bkf_[m]);
+    plan_.exec(a.data(), T(1), false);
+    for (u64 m = 0; m < n_; ++m) c[m] = scale(tmul<FWD>(a[m], bk_[m]), fct);
+  }
+
   u64 n_, n2_;
   CPack<T> plan_;
   std::vector<C<T>> bk_, bkf_;
@@ -320,7 +457,9 @@ template <class T> class CPlan {
       pack_.reset(new CPack<T>(n));
   }
   u64 length() const { return n_; }
-  void exec(C<T> *c, T fct, bool fwd) const { pack_ ? pack_->exec(c, fct, fwd) : blue_->exec(c, fct, fwd); }
+  template <class D> void exec(C<D> *c, T fct, bool fwd) const {
+    pack_ ? pack_->exec(c, fct, fwd) : blue_->exec(c, fct, fwd);
+  }
 
  private:
   u64 n_;
@@ -347,16 +486,16 @@ template <class T> class RPlan {
   }
   u64 length() const { return n_; }
 
-  void exec(T *c, T fct, bool r2hc) const {
+  template <class D> void exec(D *c, T fct, bool r2hc) const {
     const u64 n = n_;
     if (n == 1) {
-      c[0] *= fct;
+      c[0] = c[0] * fct;
       return;
     }
     if (full_) {
-      std::vector<C<T>> z(n);
+      Scratch<C<D>> z(n, kRealZ);
       if (r2hc) {
-        for (u64 j = 0; j < n; ++j) z[j] = {c[j], T(0)};
+        for (u64 j = 0; j < n; ++j) z[j] = {c[j], D{}};
         full_->exec(z.data(), fct, true);
         pack(z.data(), c);
       } else {
@@ -367,36 +506,37 @@ template <class T> class RPlan {
       return;
     }
     const u64 L = n / 2;
-    std::vector<C<T>> z(L + 1);
+    Scratch<C<D>> z(L + 1, kRealZ);
     if (r2hc) {
       for (u64 j = 0; j < L; ++j) z[j] = {c[2 * j], c[2 * j + 1]};
       half_->exec(z.data(), T(1), true);
       // split: X_k = E + W^k O, E = (Z_k + conj Z_{L-k})/2, O = (Z_k - conj Z_{L-k})/(2i)
-      std::vector<C<T>> X(L + 1);
-      X[0] = {z[0].r + z[0].i, T(0)};
-      X[L] = {z[0].r - z[0].i, T(0)};
+      Scratch<C<D>> X(L + 1, kRealX);
+      X[0] = {z[0].r + z[0].i, D{}};
+      X[L] = {z[0].r - z[0].i, D{}};
       for (u64 k = 1; k <= L / 2; ++k) {
-        const C<T> a = z[k], b = conj(z[L - k]);
-        const C<T> E = (a + b) * T(0.5);
-        const C<T> d = (a - b) * T(0.5);
-        const C<T> O = {d.i, -d.r};
-        const C<T> t = O * conj(w_[k]);  // W_n^k = e^{-2 pi i k/n}
+        const C<D> a = z[k], b = conj(z[L - k]);
+        const C<D> E = scale(a + b, T(0.5));
+        const C<D> d = scale(a - b, T(0.5));
+        const C<D> O = {d.i, -d.r};
+        const C<D> t = tmul<true>(O, w_[k]);  // W_n^k = e^{-2 pi i k/n}
         X[k] = E + t;
         X[L - k] = conj(E - t);
       }
-      for (u64 k = 0; k <= L; ++k) X[k] = X[k] * fct;
+      if (fct != T(1))
+        for (u64 k = 0; k <= L; ++k) X[k] = scale(X[k], fct);
       pack(X.data(), c);
     } else {
-      std::vector<C<T>> X(L + 1);
-      X[0] = {c[0], T(0)};
+      Scratch<C<D>> X(L + 1, kRealX);
+      X[0] = {c[0], D{}};
       for (u64 k = 1; k < L; ++k) X[k] = {c[2 * k - 1], c[2 * k]};
-      X[L] = {c[n - 1], T(0)};
+      X[L] = {c[n - 1], D{}};
       // merge: Z_k = A + u, A = X_k + conj X_{L-k}, u = i conj(W^k) (X_k - conj X_{L-k})
       for (u64 k = 0; k < L; ++k) {
-        const C<T> xk = X[k], xc = conj(X[L - k]);
-        const C<T> A = xk + xc, B = xk - xc;
-        const C<T> t = B * w_[k];  // conj(W_n^k) = e^{+2 pi i k/n}
-        z[k] = A + C<T>{-t.i, t.r};
+        const C<D> xk = X[k], xc = conj(X[L - k]);
+        const C<D> A = xk + xc, B = xk - xc;
+        const C<D> t = tmul<false>(B, w_[k]);  // conj(W_n^k) = e^{+2 pi i k/n}
+        z[k] = A + C<D>{-t.i, t.r};
       }
       half_->exec(z.data(), fct, false);
       for (u64 j = 0; j < L; ++j) {
@@ -407,7 +547,7 @@ template <class T> class RPlan {
   }
 
  private:
-  void pack(const C<T> *X, T *c) const {
+  template <class D> void pack(const C<D> *X, D *c) const {
     c[0] = X[0].r;
     u64 i = 1, k = 1;
     for (; i + 1 < n_; i += 2, ++k) {
@@ -416,15 +556,15 @@ template <class T> class RPlan {
     }
     if (i < n_) c[i] = X[k].r;
   }
-  void unpack_full(const T *c, C<T> *z) const {
+  template <class D> void unpack_full(const D *c, C<D> *z) const {
     const u64 n = n_;
-    z[0] = {c[0], T(0)};
+    z[0] = {c[0], D{}};
     u64 i = 1, k = 1;
     for (; i + 1 < n; i += 2, ++k) {
       z[k] = {c[i], c[i + 1]};
       z[n - k] = {c[i], -c[i + 1]};
     }
-    if (i < n) z[k] = {c[i], T(0)};
+    if (i < n) z[k] = {c[i], D{}};
   }
 
   u64 n_;
@@ -442,14 +582,14 @@ template <class T> class Dct1 {  // HDR:2918-2955: rfft of the even extension, l
  public:
   explicit Dct1(u64 n) : fft_(2 * (n - 1)) {}
   u64 length() const { return fft_.length() / 2 + 1; }
-  void exec(T *c, T fct, bool ortho, int, bool) const {
+  template <class D> void exec(D *c, T fct, bool ortho, int, bool) const {
     const u64 N = fft_.length(), n = N / 2 + 1;
     const T s2 = T(kSqrt2);
     if (ortho) {
       c[0] *= s2;
       c[n - 1] *= s2;
     }
-    std::vector<T> t(N);
+    Scratch<D> t(N, kDcst);
     t[0] = c[0];
     for (u64 i = 1; i < n; ++i) t[i] = t[N - i] = c[i];
     fft_.exec(t.data(), fct, true);
@@ -469,9 +609,9 @@ template <class T> class Dst1 {  // HDR:2957-2985: rfft of the odd extension, le
  public:
   explicit Dst1(u64 n) : fft_(2 * (n + 1)) {}
   u64 length() const { return fft_.length() / 2 - 1; }
-  void exec(T *c, T fct, bool, int, bool) const {
+  template <class D> void exec(D *c, T fct, bool, int, bool) const {
     const u64 N = fft_.length(), n = N / 2 - 1;
-    std::vector<T> t(N);
+    Scratch<D> t(N, kDcst);
     t[0] = t[n + 1] = c[0] * T(0);
     for (u64 i = 0; i < n; ++i) {
       t[i + 1] = c[i];
@@ -491,23 +631,23 @@ template <class T> class Dcst23 {  // HDR:2987-3061
     for (u64 i = 0; i < n; ++i) tw_[i] = unit<T>(i + 1, 4 * n).r;  // cos(2 pi (i+1) / 4n)
   }
   u64 length() const { return fft_.length(); }
-  void exec(T *c, T fct, bool ortho, int type, bool cosine) const {
+  template <class D> void exec(D *c, T fct, bool ortho, int type, bool cosine) const {
     const u64 N = length(), NS2 = (N + 1) / 2;
     const T s2 = T(kSqrt2);
     if (type == 2) {
       if (!cosine)
         for (u64 k = 1; k < N; k += 2) c[k] = -c[k];
-      c[0] *= 2;
-      if ((N & 1) == 0) c[N - 1] *= 2;
+      c[0] *= T(2);
+      if ((N & 1) == 0) c[N - 1] *= T(2);
       for (u64 k = 1; k + 1 < N; k += 2) {  // MPINPLACE(c[k+1], c[k]): (a, b) <- (a-b, a+b)
-        const T a = c[k + 1], b = c[k];
+        const D a = c[k + 1], b = c[k];
         c[k + 1] = a - b;
         c[k] = a + b;
       }
       fft_.exec(c, fct, false);
       for (u64 k = 1, kc = N - 1; k < NS2; ++k, --kc) {
-        const T t1 = tw_[k - 1] * c[kc] + tw_[kc - 1] * c[k];
-        const T t2 = tw_[k - 1] * c[k] - tw_[kc - 1] * c[kc];
+        const D t1 = tw_[k - 1] * c[kc] + tw_[kc - 1] * c[k];
+        const D t2 = tw_[k - 1] * c[k] - tw_[kc - 1] * c[kc];
         c[k] = T(0.5) * (t1 + t2);
         c[kc] = T(0.5) * (t1 - t2);
       }
@@ -520,14 +660,14 @@ template <class T> class Dcst23 {  // HDR:2987-3061
       if (!cosine)
         for (u64 k = 0, kc = N - 1; k < NS2; ++k, --kc) std::swap(c[k], c[kc]);
       for (u64 k = 1, kc = N - 1; k < NS2; ++k, --kc) {
-        const T t1 = c[k] + c[kc], t2 = c[k] - c[kc];
+        const D t1 = c[k] + c[kc], t2 = c[k] - c[kc];
         c[k] = tw_[k - 1] * t2 + tw_[kc - 1] * t1;
         c[kc] = tw_[k - 1] * t1 - tw_[kc - 1] * t2;
       }
-      if ((N & 1) == 0) c[NS2] *= 2 * tw_[NS2 - 1];
+      if ((N & 1) == 0) c[NS2] *= T(2) * tw_[NS2 - 1];
       fft_.exec(c, fct, true);
       for (u64 k = 1; k + 1 < N; k += 2) {  // MPINPLACE(c[k], c[k+1]): (a, b) <- (a-b, a+b)
-        const T a = c[k], b = c[k + 1];
+        const D a = c[k], b = c[k + 1];
         c[k] = a - b;
         c[k + 1] = a + b;
       }
@@ -552,14 +692,14 @@ template <class T> class Dcst4 {  // HDR:3063-3163
     }
   }
   u64 length() const { return N_; }
-  void exec(T *c, T fct, bool, int, bool cosine) const {
+  template <class D> void exec(D *c, T fct, bool, int, bool cosine) const {
     const u64 N = N_, n2 = N / 2;
     if (!cosine)
       for (u64 k = 0, kc = N - 1; k < n2; ++k, --kc) std::swap(c[k], c[kc]);
     if (N & 1) {
       // odd length: the index shuffle and sign pattern of the reference (derived there from
       // FFTW's apply_re11) around a real FFT of length N
-      std::vector<T> y(N);
+      Scratch<D> y(N, kDcst);
       {
         u64 i = 0, m = n2;
         for (; m < N; ++i, m += 4) y[i] = c[m];
@@ -584,12 +724,12 @@ template <class T> class Dcst4 {  // HDR:3063-3163
       }
     } else {
       // even length: half-length complex FFT between two twiddle multiplies
-      std::vector<C<T>> y(n2);
-      for (u64 i = 0; i < n2; ++i) y[i] = C<T>{c[2 * i], c[N - 1 - i * 2]} * C2_[i];
+      Scratch<C<D>> y(n2, kDcst);
+      for (u64 i = 0; i < n2; ++i) y[i] = tmul<false>(C<D>{c[2 * i], c[N - 1 - i * 2]}, C2_[i]);
       fft_->exec(y.data(), fct, true);
       for (u64 i = 0, ic = n2 - 1; i < n2; ++i, --ic) {
-        c[2 * i] = 2 * (y[i].r * C2_[i].r - y[i].i * C2_[i].i);
-        c[2 * i + 1] = -2 * (y[ic].i * C2_[ic].r + y[ic].r * C2_[ic].i);
+        c[2 * i] = T(2) * (y[i].r * C2_[i].r - y[i].i * C2_[i].i);
+        c[2 * i + 1] = T(-2) * (y[ic].i * C2_[ic].r + y[ic].r * C2_[ic].i);
       }
     }
     if (!cosine)
@@ -628,50 +768,147 @@ struct View {
 };
 
 // thread count rule of util::thread_count (HDR:712-723)
-static u64 thread_count(u64 nthreads, const std::vector<i64> &shape, size_t axis) {
+static u64 thread_count(u64 nthreads, const std::vector<i64> &shape, size_t axis, u64 vlen) {
   if (nthreads == 1) return 1;
   u64 size = 1;
   for (i64 s : shape) size *= u64(s);
-  u64 parallel = size / u64(shape[axis]);
+  u64 parallel = size / (u64(shape[axis]) * vlen);
   if (shape[axis] < 1000) parallel /= 4;
   const u64 mx = nthreads == 0 ? std::max(1u, std::thread::hardware_concurrency()) : nthreads;
   return std::max<u64>(1, std::min(parallel, mx));
 }
 
-// Calls f(in_offset, out_offset) for every row along `axis` (C order of the other dims),
-// spreading rows over threads.
-template <class F>
+// Persistent worker threads for the row loops (the reference keeps a thread pool too,
+// HDR:760-960): run(nt, fn) calls fn(0..nt-1), index 0 on the calling thread, and returns when
+// all are done. One job at a time; a child process after fork() builds its own pool.
+class Pool {
+ public:
+  static Pool &get() {
+    static Pool *pool = nullptr;
+    static pid_t owner = 0;
+    if (pool == nullptr || owner != getpid()) {  // the parent's workers do not exist after fork
+      pool = new Pool();
+      owner = getpid();
+    }
+    return *pool;
+  }
+  void run(u64 nt, const std::function<void(u64)> &fn) {
+    std::lock_guard<std::mutex> job(job_mu_);
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      while (workers_.size() + 1 < nt) workers_.emplace_back([this] { loop(); });
+      fn_ = &fn;
+      count_ = nt;
+      next_ = 1;
+      left_ = nt - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    fn(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [&] { return left_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  void loop() {
+    u64 seen = 0;
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      cv_.wait(lk, [&] { return gen_ != seen; });
+      seen = gen_;
+      while (fn_ != nullptr && next_ < count_) {
+        const u64 i = next_++;
+        const std::function<void(u64)> *fn = fn_;
+        lk.unlock();
+        (*fn)(i);
+        lk.lock();
+        if (--left_ == 0) done_.notify_all();
+      }
+    }
+  }
+  std::mutex job_mu_, mu_;
+  std::condition_variable cv_, done_;
+  std::vector<std::thread> workers_;
+  const std::function<void(u64)> *fn_ = nullptr;
+  u64 count_ = 0, next_ = 0, left_ = 0, gen_ = 0;
+};
+
+// Calls f(in_offsets, out_offsets, G, lanes) for the rows along `axis` (C order of the other
+// dims): G groups of W consecutive rows (lanes = integral_constant<int, W>, G <= gmax) while W
+// rows remain in a thread's share, then single rows (lanes = integral_constant<int, 1>, G = 1).
+// Rows are spread over threads.
+constexpr int kMaxRows = 64;
+template <int W, class F>
 static void for_rows(const std::vector<i64> &shape, const std::vector<i64> &sin, const std::vector<i64> &sout,
-                     size_t axis, u64 nthreads, F f) {
+                     size_t axis, u64 nthreads, int gmax, F f) {
   const size_t nd = shape.size();
   u64 rows = 1;
   for (size_t d = 0; d < nd; ++d)
     if (d != axis) rows *= u64(shape[d]);
-  const u64 nt = thread_count(nthreads, shape, axis);
+  const u64 nt = thread_count(nthreads, shape, axis, W);
+  auto offsets = [&](u64 r, i64 &oi, i64 &oo) {
+    u64 rem = r;
+    oi = oo = 0;
+    for (size_t dd = nd; dd-- > 0;) {
+      if (dd == axis) continue;
+      const u64 pos = rem % u64(shape[dd]);
+      rem /= u64(shape[dd]);
+      oi += i64(pos) * sin[dd];
+      oo += i64(pos) * sout[dd];
+    }
+  };
   auto work = [&](u64 lo, u64 hi) {
-    for (u64 r = lo; r < hi; ++r) {
-      u64 rem = r;
-      i64 oi = 0, oo = 0;
-      for (size_t dd = nd; dd-- > 0;) {
-        if (dd == axis) continue;
-        const u64 pos = rem % u64(shape[dd]);
-        rem /= u64(shape[dd]);
-        oi += i64(pos) * sin[dd];
-        oo += i64(pos) * sout[dd];
+    i64 oi[kMaxRows], oo[kMaxRows];
+    u64 r = lo;
+    if constexpr (W > 1) {
+      while (r + W <= hi) {
+        const int G = int(std::min<u64>(u64(gmax), (hi - r) / W));
+        for (int l = 0; l < G * W; ++l) offsets(r + u64(l), oi[l], oo[l]);
+        f(oi, oo, G, std::integral_constant<int, W>{});
+        r += u64(G) * W;
       }
-      f(oi, oo);
+    }
+    for (; r < hi; ++r) {
+      offsets(r, oi[0], oo[0]);
+      f(oi, oo, 1, std::integral_constant<int, 1>{});
     }
   };
   if (nt <= 1) {
     work(0, rows);
     return;
   }
-  std::vector<std::thread> th;
-  for (u64 t = 0; t < nt; ++t) {
-    const u64 lo = rows * t / nt, hi = rows * (t + 1) / nt;
-    th.emplace_back(work, lo, hi);
-  }
-  for (auto &x : th) x.join();
+  Pool::get().run(nt, [&](u64 t) { work(rows * t / nt, rows * (t + 1) / nt); });
+}
+
+// Groups of W rows taken per call: one for a contiguous axis; for a strided one enough that the
+// rows cover 128 contiguous bytes, so that every cache line gathered from (or scattered to) the
+// array is used whole at once, before the other rows' lines can evict it (with power-of-two
+// strides all of a row's elements fall into one cache set).
+template <int W> static int groups_for(i64 si, i64 so, size_t elem) {
+  if (si == i64(elem) && so == i64(elem)) return 1;
+  return std::max(1, std::min(kMaxRows / W, int(128 / (W * elem))));
+}
+
+// Real rows: gather G groups of W rows (element j of row g W + l at base[g W + l] + j * stride)
+// into lane vectors t[g n + j], and scatter them back.
+template <class T, int W>
+static void gather_real(typename Lanes<T, W>::D *t, const char *d, const i64 *base, i64 stride, u64 n, int G) {
+  for (u64 j = 0; j < n; ++j)
+    for (int g = 0; g < G; ++g) {
+      typename Lanes<T, W>::D v;
+      for (int l = 0; l < W; ++l)
+        Lanes<T, W>::set(v, l, *reinterpret_cast<const T *>(d + base[g * W + l] + i64(j) * stride));
+      t[size_t(g) * n + j] = v;
+    }
+}
+template <class T, int W>
+static void scatter_real(const typename Lanes<T, W>::D *t, char *d, const i64 *base, i64 stride, u64 n, int G) {
+  for (u64 j = 0; j < n; ++j)
+    for (int g = 0; g < G; ++g) {
+      const typename Lanes<T, W>::D v = t[size_t(g) * n + j];
+      for (int l = 0; l < W; ++l) *reinterpret_cast<T *>(d + base[g * W + l] + i64(j) * stride) = Lanes<T, W>::get(v, l);
+    }
 }
 
 static bool any_zero(const std::vector<i64> &s) {
@@ -690,18 +927,29 @@ static void c2c_nd(const View &in, const View &out, const std::vector<u64> &axes
     auto plan = get_plan<CPlan<T>>(n);
     const i64 si = src.stride[ax], so = out.stride[ax];
     const T f = k == 0 ? fct : T(1);
-    for_rows(in.shape, src.stride, out.stride, ax, nth, [&](i64 oi, i64 oo) {
-      std::vector<C<T>> buf(n);
-      for (u64 j = 0; j < n; ++j) {
-        const T *p = reinterpret_cast<const T *>(src.d + oi + i64(j) * si);
-        buf[j] = {p[0], p[1]};
-      }
-      plan->exec(buf.data(), f, fwd);
-      for (u64 j = 0; j < n; ++j) {
-        T *p = reinterpret_cast<T *>(out.d + oo + i64(j) * so);
-        p[0] = buf[j].r;
-        p[1] = buf[j].i;
-      }
+    const int gmax = groups_for<kLanes<T>>(si, so, sizeof(C<T>));
+    for_rows<kLanes<T>>(in.shape, src.stride, out.stride, ax, nth, gmax,
+                        [&](const i64 *oi, const i64 *oo, int G, auto lanes) {
+      constexpr int W = decltype(lanes)::value;
+      using LN = Lanes<T, W>;
+      Scratch<C<typename LN::D>> buf(size_t(G) * n, kRows);
+      for (u64 j = 0; j < n; ++j)  // lanes composed in registers, one store per vector
+        for (int g = 0; g < G; ++g) {
+          typename LN::D re, im;
+          for (int l = 0; l < W; ++l) {
+            const C<T> x = *reinterpret_cast<const C<T> *>(src.d + oi[g * W + l] + i64(j) * si);
+            LN::set(re, l, x.r);
+            LN::set(im, l, x.i);
+          }
+          buf[size_t(g) * n + j] = {re, im};
+        }
+      for (int g = 0; g < G; ++g) plan->exec(buf.data() + size_t(g) * n, f, fwd);
+      for (u64 j = 0; j < n; ++j)
+        for (int g = 0; g < G; ++g) {
+          const C<typename LN::D> v = buf[size_t(g) * n + j];
+          for (int l = 0; l < W; ++l)
+            *reinterpret_cast<C<T> *>(out.d + oo[g * W + l] + i64(j) * so) = C<T>{LN::get(v.r, l), LN::get(v.i, l)};
+        }
     });
   }
 }
@@ -709,43 +957,74 @@ static void c2c_nd(const View &in, const View &out, const std::vector<u64> &axes
 // general_r2c (HDR:3723-3779): halfcomplex to complex, conjugated when !forward
 template <class T>
 static void r2c_axis(const View &in, const View &out, size_t ax, bool fwd, T fct, u64 nth) {
-  const u64 n = u64(in.shape[ax]);
+  const u64 n = u64(in.shape[ax]), nout = n / 2 + 1;
   auto plan = get_plan<RPlan<T>>(n);
   const i64 si = in.stride[ax], so = out.stride[ax];
-  for_rows(in.shape, in.stride, out.stride, ax, nth, [&](i64 oi, i64 oo) {
-    std::vector<T> t(n);
-    for (u64 j = 0; j < n; ++j) t[j] = *reinterpret_cast<const T *>(in.d + oi + i64(j) * si);
-    plan->exec(t.data(), fct, true);
-    auto put = [&](u64 k, T re, T im) {
-      T *p = reinterpret_cast<T *>(out.d + oo + i64(k) * so);
+  const int gmax = groups_for<kLanes<T>>(si == i64(sizeof(T)) ? i64(sizeof(C<T>)) : si, so, sizeof(C<T>));
+  for_rows<kLanes<T>>(in.shape, in.stride, out.stride, ax, nth, gmax,
+                      [&](const i64 *oi, const i64 *oo, int G, auto lanes) {
+    constexpr int W = decltype(lanes)::value;
+    using LN = Lanes<T, W>;
+    Scratch<typename LN::D> t(size_t(G) * n, kRows);
+    gather_real<T, W>(t.data(), in.d, oi, si, n, G);
+    for (int g = 0; g < G; ++g) plan->exec(t.data() + size_t(g) * n, fct, true);
+    // bin k from the half-complex row: (t_0, 0), (t_{2k-1}, t_{2k}), and (t_{n-1}, 0) at k = n/2
+    // for even n
+    auto put = [&](u64 k, int g, int l) {
+      const typename LN::D *row = t.data() + size_t(g) * n;
+      const T re = LN::get(row[k == 0 ? 0 : 2 * k - 1], l);
+      const T im = (k == 0 || 2 * k >= n) ? T(0) : LN::get(row[2 * k], l);
+      T *p = reinterpret_cast<T *>(out.d + oo[g * W + l] + i64(k) * so);
       p[0] = re;
       p[1] = fwd ? im : -im;
     };
-    put(0, t[0], T(0));
-    u64 i = 1, k = 1;
-    for (; i + 1 < n; i += 2, ++k) put(k, t[i], t[i + 1]);
-    if (i < n) put(k, t[i], T(0));
+    if (so == i64(sizeof(C<T>))) {  // contiguous output rows: one row after the other
+      for (int g = 0; g < G; ++g)
+        for (int l = 0; l < W; ++l)
+          for (u64 k = 0; k < nout; ++k) put(k, g, l);
+    } else {  // strided: bin by bin across the rows
+      for (u64 k = 0; k < nout; ++k)
+        for (int g = 0; g < G; ++g)
+          for (int l = 0; l < W; ++l) put(k, g, l);
+    }
   });
 }
 
 // general_c2r (HDR:3780-3852): imaginary parts negated when forward
 template <class T>
 static void c2r_axis(const View &in, const View &out, size_t ax, bool fwd, T fct, u64 nth) {
-  const u64 n = u64(out.shape[ax]);
+  const u64 n = u64(out.shape[ax]), nin = n / 2 + 1;
   auto plan = get_plan<RPlan<T>>(n);
   const i64 si = in.stride[ax], so = out.stride[ax];
-  for_rows(out.shape, in.stride, out.stride, ax, nth, [&](i64 oi, i64 oo) {
-    std::vector<T> t(n);
-    auto get = [&](u64 k) { return reinterpret_cast<const T *>(in.d + oi + i64(k) * si); };
-    t[0] = get(0)[0];
-    u64 i = 1, k = 1;
-    for (; i + 1 < n; i += 2, ++k) {
-      t[i] = get(k)[0];
-      t[i + 1] = fwd ? -get(k)[1] : get(k)[1];
+  const int gmax = groups_for<kLanes<T>>(si, so == i64(sizeof(T)) ? i64(sizeof(C<T>)) : so, sizeof(C<T>));
+  for_rows<kLanes<T>>(out.shape, in.stride, out.stride, ax, nth, gmax,
+                      [&](const i64 *oi, const i64 *oo, int G, auto lanes) {
+    constexpr int W = decltype(lanes)::value;
+    using LN = Lanes<T, W>;
+    Scratch<typename LN::D> t(size_t(G) * n, kRows);
+    // half-complex row from the bins: t_0 = Re X_0, (t_{2k-1}, t_{2k}) = X_k, t_{n-1} = Re X_{n/2}
+    // for even n
+    auto get = [&](u64 k, int g, int l) {
+      typename LN::D *row = t.data() + size_t(g) * n;
+      const T *p = reinterpret_cast<const T *>(in.d + oi[g * W + l] + i64(k) * si);
+      if (k == 0) {
+        LN::set(row[0], l, p[0]);
+      } else {
+        LN::set(row[2 * k - 1], l, p[0]);
+        if (2 * k < n) LN::set(row[2 * k], l, fwd ? -p[1] : p[1]);
+      }
+    };
+    if (si == i64(sizeof(C<T>))) {  // contiguous input rows: one row after the other
+      for (int g = 0; g < G; ++g)
+        for (int l = 0; l < W; ++l)
+          for (u64 k = 0; k < nin; ++k) get(k, g, l);
+    } else {  // strided: bin by bin across the rows
+      for (u64 k = 0; k < nin; ++k)
+        for (int g = 0; g < G; ++g)
+          for (int l = 0; l < W; ++l) get(k, g, l);
     }
-    if (i < n) t[i] = get(k)[0];
-    plan->exec(t.data(), fct, false);
-    for (u64 j = 0; j < n; ++j) *reinterpret_cast<T *>(out.d + oo + i64(j) * so) = t[j];
+    for (int g = 0; g < G; ++g) plan->exec(t.data() + size_t(g) * n, fct, false);
+    scatter_real<T, W>(t.data(), out.d, oo, so, n, G);
   });
 }
 
@@ -774,8 +1053,8 @@ static void c2r_nd(const View &in, const View &out, const std::vector<u64> &axes
   // c2c over the other axes into a C-contiguous temporary (HDR:4009-4020)
   u64 total = 1;
   for (i64 s : i2.shape) total *= u64(s);
-  std::vector<C<T>> tmp(total);
-  View t{reinterpret_cast<char *>(tmp.data()), i2.shape, std::vector<i64>(i2.shape.size())};
+  std::unique_ptr<C<T>[]> tmp(new C<T>[total]);  // every element is written by the c2c below
+  View t{reinterpret_cast<char *>(tmp.get()), i2.shape, std::vector<i64>(i2.shape.size())};
   i64 acc = sizeof(C<T>);
   for (size_t d = i2.shape.size(); d-- > 0;) {
     t.stride[d] = acc;
@@ -838,11 +1117,14 @@ static void dcst_nd(const View &in, const View &out, const std::vector<u64> &axe
     auto plan = get_plan<P>(n);
     const i64 si = src.stride[ax], so = out.stride[ax];
     const T f = k == 0 ? fct : T(1);
-    for_rows(in.shape, src.stride, out.stride, ax, nth, [&](i64 oi, i64 oo) {
-      std::vector<T> t(n);
-      for (u64 j = 0; j < n; ++j) t[j] = *reinterpret_cast<const T *>(src.d + oi + i64(j) * si);
-      plan->exec(t.data(), f, ortho, type, cosine);
-      for (u64 j = 0; j < n; ++j) *reinterpret_cast<T *>(out.d + oo + i64(j) * so) = t[j];
+    const int gmax = groups_for<kLanes<T>>(si, so, sizeof(T));
+    for_rows<kLanes<T>>(in.shape, src.stride, out.stride, ax, nth, gmax,
+                        [&](const i64 *oi, const i64 *oo, int G, auto lanes) {
+      constexpr int W = decltype(lanes)::value;
+      Scratch<typename Lanes<T, W>::D> t(size_t(G) * n, kRows);
+      gather_real<T, W>(t.data(), src.d, oi, si, n, G);
+      for (int g = 0; g < G; ++g) plan->exec(t.data() + size_t(g) * n, f, ortho, type, cosine);
+      scatter_real<T, W>(t.data(), out.d, oo, so, n, G);
     });
   }
 }
@@ -876,15 +1158,21 @@ static void r2r_fftpack(const View &in, const View &out, const std::vector<u64> 
     auto plan = get_plan<RPlan<T>>(n);
     const i64 si = src.stride[ax], so = out.stride[ax];
     const T f = k == 0 ? fct : T(1);
-    for_rows(in.shape, src.stride, out.stride, ax, nth, [&](i64 oi, i64 oo) {
-      std::vector<T> t(n);
-      for (u64 j = 0; j < n; ++j) t[j] = *reinterpret_cast<const T *>(src.d + oi + i64(j) * si);
-      if (!r2h && fwd)
-        for (u64 i = 2; i < n; i += 2) t[i] = -t[i];
-      plan->exec(t.data(), f, fwd);
-      if (r2h && !fwd)
-        for (u64 i = 2; i < n; i += 2) t[i] = -t[i];
-      for (u64 j = 0; j < n; ++j) *reinterpret_cast<T *>(out.d + oo + i64(j) * so) = t[j];
+    const int gmax = groups_for<kLanes<T>>(si, so, sizeof(T));
+    for_rows<kLanes<T>>(in.shape, src.stride, out.stride, ax, nth, gmax,
+                        [&](const i64 *oi, const i64 *oo, int G, auto lanes) {
+      constexpr int W = decltype(lanes)::value;
+      Scratch<typename Lanes<T, W>::D> t(size_t(G) * n, kRows);
+      gather_real<T, W>(t.data(), src.d, oi, si, n, G);
+      for (int g = 0; g < G; ++g) {
+        typename Lanes<T, W>::D *row = t.data() + size_t(g) * n;
+        if (!r2h && fwd)
+          for (u64 i = 2; i < n; i += 2) row[i] = -row[i];
+        plan->exec(row, f, fwd);
+        if (r2h && !fwd)
+          for (u64 i = 2; i < n; i += 2) row[i] = -row[i];
+      }
+      scatter_real<T, W>(t.data(), out.d, oo, so, n, G);
     });
   }
 }
@@ -900,18 +1188,32 @@ static void hartley_sep(const View &in, const View &out, const std::vector<u64> 
     auto plan = get_plan<RPlan<T>>(n);
     const i64 si = src.stride[ax], so = out.stride[ax];
     const T f = k == 0 ? fct : T(1);
-    for_rows(in.shape, src.stride, out.stride, ax, nth, [&](i64 oi, i64 oo) {
-      std::vector<T> t(n);
-      for (u64 j = 0; j < n; ++j) t[j] = *reinterpret_cast<const T *>(src.d + oi + i64(j) * si);
-      plan->exec(t.data(), f, true);
-      auto at = [&](u64 j) -> T & { return *reinterpret_cast<T *>(out.d + oo + i64(j) * so); };
-      at(0) = t[0];
-      u64 i = 1, i1 = 1, i2 = n - 1;
-      for (; i + 1 < n; i += 2, ++i1, --i2) {
-        at(i1) = t[i] + t[i + 1];
-        at(i2) = t[i] - t[i + 1];
-      }
-      if (i < n) at(i1) = t[i];
+    const int gmax = groups_for<kLanes<T>>(si, so, sizeof(T));
+    for_rows<kLanes<T>>(in.shape, src.stride, out.stride, ax, nth, gmax,
+                        [&](const i64 *oi, const i64 *oo, int G, auto lanes) {
+      constexpr int W = decltype(lanes)::value;
+      using LN = Lanes<T, W>;
+      Scratch<typename LN::D> t(size_t(G) * n, kRows);
+      gather_real<T, W>(t.data(), src.d, oi, si, n, G);
+      for (int g = 0; g < G; ++g) plan->exec(t.data() + size_t(g) * n, f, true);
+      // out_0 = t_0, out_k = t_{2k-1} + t_{2k}, out_{n-k} = t_{2k-1} - t_{2k}, and
+      // out_{n/2} = t_{n-1} for even n
+      for (u64 k = 0; k <= n / 2; ++k)
+        for (int g = 0; g < G; ++g) {
+          const typename LN::D *row = t.data() + size_t(g) * n;
+          for (int l = 0; l < W; ++l) {
+            auto at = [&](u64 j) -> T & { return *reinterpret_cast<T *>(out.d + oo[g * W + l] + i64(j) * so); };
+            if (k == 0) {
+              at(0) = LN::get(row[0], l);
+            } else if (2 * k < n) {
+              const T a = LN::get(row[2 * k - 1], l), b = LN::get(row[2 * k], l);
+              at(k) = a + b;
+              at(n - k) = a - b;
+            } else {
+              at(k) = LN::get(row[2 * k - 1], l);
+            }
+          }
+        }
     });
   }
 }
