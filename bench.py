@@ -271,7 +271,7 @@ def run_c1(args):
     cpu_rate = 5 * 256 / (time.perf_counter() - t0)
     hx = torch.empty(shape, dtype=torch.complex128, pin_memory=True)
     hx.copy_(xs[0].cpu())
-    hy = torch.empty_like(hx)
+    hy = torch.empty(shape, dtype=torch.complex128, pin_memory=True)
     nx, ny = hx.numpy(), hy.numpy()
     rg.set_stream(None)
     rg.c2c(nx, ny, axes, True, 1.0, 1)
