@@ -273,103 +273,6 @@ bool pipeline_ok(const Desc &din, const Desc &dout, const std::vector<uint64_t> 
   return is_pinned_host(din.data) && is_pinned_host(dout.data);
 }
 
-// r2c (forward, fct) of host din into host dout, pipelined as described above.
-void pipelined_r2c(DType dt, const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax, bool forward,
-                   double fct) {
-  cudaStream_t st = t_stream, cs = copy_stream();
-  const int64_t n0 = din.shape[0];
-  const int64_t plane_in = din.bstride[0], plane_out = dout.bstride[0];
-  rg::DevBuf bin(size_t(n0 * plane_in), st), bout(size_t(n0 * plane_out), st);
-  cudaEvent_t ready;
-  RG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-  RG_CUDA(cudaEventRecord(ready, st));  // the buffers exist in st's order
-  RG_CUDA(cudaStreamWaitEvent(cs, ready, 0));
-  const int64_t K = std::min<int64_t>(4, n0), per = (n0 + K - 1) / K;
-  std::vector<cudaEvent_t> arrived;
-  const rg::Axes rest(ax.begin() + 1, ax.end());
-  for (int64_t c0 = 0; c0 < n0; c0 += per) {
-    const int64_t cn = std::min(per, n0 - c0);
-    cudaEvent_t ev;
-    RG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(bin.get()) + c0 * plane_in,
-                            static_cast<const char *>(din.data) + c0 * plane_in, size_t(cn * plane_in),
-                            cudaMemcpyHostToDevice, cs));
-    RG_CUDA(cudaEventRecord(ev, cs));
-    arrived.push_back(ev);
-    RG_CUDA(cudaStreamWaitEvent(st, ev, 0));
-    std::vector<int64_t> si = din.shape, so = dout.shape;
-    si[0] = so[0] = cn;
-    rg::exec_r2c(dt, dense_view(static_cast<char *>(bin.get()) + c0 * plane_in, si),
-                 dense_view(static_cast<char *>(bout.get()) + c0 * plane_out, so), rest, forward, fct, st);
-  }
-  const NdArray whole = dense_view(bout.get(), dout.shape);
-  rg::exec_c2c(dt, whole, whole, rg::Axes{0}, forward, 1.0, st);
-  RG_CUDA(cudaMemcpyAsync(dout.data, bout.get(), size_t(n0 * plane_out), cudaMemcpyDeviceToHost, st));
-  RG_CUDA(cudaStreamSynchronize(st));
-  for (cudaEvent_t e : arrived) cudaEventDestroy(e);
-  cudaEventDestroy(ready);
-}
-
-// c2r (forward, fct) of host din into host dout, pipelined as described above.
-void pipelined_c2r(DType dt, const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax, bool forward,
-                   double fct) {
-  cudaStream_t st = t_stream, cs = copy_stream();
-  const int64_t n0 = dout.shape[0];
-  const int64_t plane_in = din.bstride[0], plane_out = dout.bstride[0];
-  rg::DevBuf bin(size_t(n0 * plane_in), st), bout(size_t(n0 * plane_out), st);
-  RG_CUDA(cudaMemcpyAsync(bin.get(), din.data, size_t(n0 * plane_in), cudaMemcpyHostToDevice, st));
-  const NdArray whole = dense_view(bin.get(), din.shape);
-  rg::exec_c2c(dt, whole, whole, rg::Axes{0}, forward, 1.0, st);  // in place on the staging copy
-  const int64_t K = std::min<int64_t>(4, n0), per = (n0 + K - 1) / K;
-  const rg::Axes rest(ax.begin() + 1, ax.end());
-  std::vector<cudaEvent_t> done;
-  for (int64_t c0 = 0; c0 < n0; c0 += per) {
-    const int64_t cn = std::min(per, n0 - c0);
-    std::vector<int64_t> si = din.shape, so = dout.shape;
-    si[0] = so[0] = cn;
-    rg::exec_c2r(dt, dense_view(static_cast<char *>(bin.get()) + c0 * plane_in, si),
-                 dense_view(static_cast<char *>(bout.get()) + c0 * plane_out, so), rest, forward, fct, st);
-    cudaEvent_t ev;
-    RG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    RG_CUDA(cudaEventRecord(ev, st));
-    done.push_back(ev);
-    RG_CUDA(cudaStreamWaitEvent(cs, ev, 0));
-    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(dout.data) + c0 * plane_out,
-                            static_cast<char *>(bout.get()) + c0 * plane_out, size_t(cn * plane_out),
-                            cudaMemcpyDeviceToHost, cs));
-  }
-  RG_CUDA(cudaStreamSynchronize(cs));
-  // the buffers go back to the pool in st's order once the copies on cs are done
-  cudaEvent_t fin;
-  RG_CUDA(cudaEventCreateWithFlags(&fin, cudaEventDisableTiming));
-  RG_CUDA(cudaEventRecord(fin, cs));
-  RG_CUDA(cudaStreamWaitEvent(st, fin, 0));
-  for (cudaEvent_t e : done) cudaEventDestroy(e);
-  cudaEventDestroy(fin);
-}
-
-// ---- host arrays with a batch dimension: copy-in, compute and copy-out overlapped ----
-//
-// When the outermost dimension is not transformed, its slabs are independent transforms. A
-// host call then runs as a three-stage pipeline: slab i is copied in on the copy-in stream,
-// transformed on one of two compute streams as soon as it has arrived, and copied out on the
-// copy-out stream, while slab i+1 is copied in and slab i-1 copied out; the two link
-// directions run at once. Dense C-order host arrays only (every slab is one contiguous range
-// of both arrays), and only when the copies are large enough to matter.
-
-bool slabs_ok(const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax) {
-  if (din.shape.empty() || din.shape[0] < 2 || dout.shape.empty() || dout.shape[0] != din.shape[0]) return false;
-  for (uint64_t a : ax)
-    if (a == 0) return false;
-  if (!din.data || !dout.data || !dense_c(din) || !dense_c(dout)) return false;
-  const int64_t bytes = din.shape[0] * din.bstride[0] + dout.shape[0] * dout.bstride[0];
-  if (bytes < (int64_t(2) << 20)) return false;
-  // pageable memory is copied through the driver's staging buffers, synchronously with the
-  // host: smaller copies only add overhead there (measured 310 us whole vs 499 us in 4 slabs
-  // for 256 x 4096 complex128)
-  return is_pinned_host(din.data) && is_pinned_host(dout.data);
-}
-
 // Events for the pipelines, created once per thread and device and reused by every call.
 class EventCache {
  public:
@@ -408,6 +311,140 @@ struct JoinSides {
     }
   }
 };
+
+// View of columns [j0, j0 + nj) of dimension 1 of a dense C-order array (all other dims whole).
+NdArray column_chunk(void *base, const std::vector<int64_t> &shape, int64_t itemsize, int64_t j0, int64_t nj) {
+  NdArray v = dense_view(base, shape);
+  v.data = static_cast<char *>(base) + j0 * v.stride[1] * itemsize;
+  v.shape[1] = nj;
+  return v;
+}
+
+// Slab and column-chunk counts of the three-axis pipelines.
+int64_t slab_count(int64_t n0) { return std::max<int64_t>(1, std::min<int64_t>(2 * max_slabs(), n0)); }
+int64_t chunk_count(int64_t n1) { return std::max<int64_t>(1, std::min<int64_t>(max_slabs(), n1)); }
+
+// r2c (forward, fct) of host din into host dout, pipelined as described above: slabs of planes
+// in (copy-in stream) and through the passes over every axis but the outermost; then the
+// outermost axis in column chunks along dimension 1, each chunk copied out (a 2-D copy on the
+// copy-out stream) while the next one is transformed.
+void pipelined_r2c(DType dt, const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax, bool forward,
+                   double fct) {
+  cudaStream_t st = t_stream, cin = side_stream(kCopyIn), cout = side_stream(kCopyOut);
+  const int64_t n0 = din.shape[0], n1 = dout.shape[1];
+  const int64_t plane_in = din.bstride[0], plane_out = dout.bstride[0];
+  rg::DevBuf bin(size_t(n0 * plane_in), st), bout(size_t(n0 * plane_out), st);
+  JoinSides join{st, {cin, cout}};
+  size_t ne = 0;
+  cudaEvent_t ready = t_events.get(ne++);
+  RG_CUDA(cudaEventRecord(ready, st));  // the buffers exist in st's order
+  RG_CUDA(cudaStreamWaitEvent(cin, ready, 0));
+  const int64_t K = slab_count(n0), per = (n0 + K - 1) / K;
+  const rg::Axes rest(ax.begin() + 1, ax.end());
+  for (int64_t c0 = 0; c0 < n0; c0 += per) {
+    const int64_t cn = std::min(per, n0 - c0);
+    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(bin.get()) + c0 * plane_in,
+                            static_cast<const char *>(din.data) + c0 * plane_in, size_t(cn * plane_in),
+                            cudaMemcpyHostToDevice, cin));
+    cudaEvent_t arrived = t_events.get(ne++);
+    RG_CUDA(cudaEventRecord(arrived, cin));
+    RG_CUDA(cudaStreamWaitEvent(st, arrived, 0));
+    std::vector<int64_t> si = din.shape, so = dout.shape;
+    si[0] = so[0] = cn;
+    rg::exec_r2c(dt, dense_view(static_cast<char *>(bin.get()) + c0 * plane_in, si),
+                 dense_view(static_cast<char *>(bout.get()) + c0 * plane_out, so), rest, forward, fct, st);
+  }
+  const int64_t KC = chunk_count(n1), cper = (n1 + KC - 1) / KC;
+  const int64_t row = plane_out / n1;  // bytes of one index of dimension 1
+  for (int64_t j0 = 0; j0 < n1; j0 += cper) {
+    const int64_t nj = std::min(cper, n1 - j0);
+    const NdArray v = column_chunk(bout.get(), dout.shape, dout.itemsize, j0, nj);
+    rg::exec_c2c(dt, v, v, rg::Axes{0}, forward, 1.0, st);
+    cudaEvent_t done = t_events.get(ne++);
+    RG_CUDA(cudaEventRecord(done, st));
+    RG_CUDA(cudaStreamWaitEvent(cout, done, 0));
+    RG_CUDA(cudaMemcpy2DAsync(static_cast<char *>(dout.data) + j0 * row, size_t(plane_out),
+                              static_cast<char *>(bout.get()) + j0 * row, size_t(plane_out), size_t(nj * row),
+                              size_t(n0), cudaMemcpyDeviceToHost, cout));
+  }
+  cudaEvent_t fin = t_events.get(ne++);
+  RG_CUDA(cudaEventRecord(fin, cout));
+  RG_CUDA(cudaStreamWaitEvent(st, fin, 0));
+  join.dismiss();
+  RG_CUDA(cudaEventSynchronize(fin));
+}
+
+// c2r (forward, fct) of host din into host dout, pipelined as described above: the input in
+// column chunks along dimension 1 (2-D copies on the copy-in stream), each chunk through the
+// outermost axis as soon as it has arrived (in place on the staging copy); then slabs of planes
+// through the remaining passes, each copied out while the next is transformed.
+void pipelined_c2r(DType dt, const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax, bool forward,
+                   double fct) {
+  cudaStream_t st = t_stream, cin = side_stream(kCopyIn), cout = side_stream(kCopyOut);
+  const int64_t n0 = dout.shape[0], n1 = din.shape[1];
+  const int64_t plane_in = din.bstride[0], plane_out = dout.bstride[0];
+  rg::DevBuf bin(size_t(n0 * plane_in), st), bout(size_t(n0 * plane_out), st);
+  JoinSides join{st, {cin, cout}};
+  size_t ne = 0;
+  cudaEvent_t ready = t_events.get(ne++);
+  RG_CUDA(cudaEventRecord(ready, st));
+  RG_CUDA(cudaStreamWaitEvent(cin, ready, 0));
+  const int64_t KC = chunk_count(n1), cper = (n1 + KC - 1) / KC;
+  const int64_t row = plane_in / n1;
+  for (int64_t j0 = 0; j0 < n1; j0 += cper) {
+    const int64_t nj = std::min(cper, n1 - j0);
+    RG_CUDA(cudaMemcpy2DAsync(static_cast<char *>(bin.get()) + j0 * row, size_t(plane_in),
+                              static_cast<const char *>(din.data) + j0 * row, size_t(plane_in), size_t(nj * row),
+                              size_t(n0), cudaMemcpyHostToDevice, cin));
+    cudaEvent_t arrived = t_events.get(ne++);
+    RG_CUDA(cudaEventRecord(arrived, cin));
+    RG_CUDA(cudaStreamWaitEvent(st, arrived, 0));
+    const NdArray v = column_chunk(bin.get(), din.shape, din.itemsize, j0, nj);
+    rg::exec_c2c(dt, v, v, rg::Axes{0}, forward, 1.0, st);  // in place on the staging copy
+  }
+  const int64_t K = slab_count(n0), per = (n0 + K - 1) / K;
+  const rg::Axes rest(ax.begin() + 1, ax.end());
+  for (int64_t c0 = 0; c0 < n0; c0 += per) {
+    const int64_t cn = std::min(per, n0 - c0);
+    std::vector<int64_t> si = din.shape, so = dout.shape;
+    si[0] = so[0] = cn;
+    rg::exec_c2r(dt, dense_view(static_cast<char *>(bin.get()) + c0 * plane_in, si),
+                 dense_view(static_cast<char *>(bout.get()) + c0 * plane_out, so), rest, forward, fct, st);
+    cudaEvent_t done = t_events.get(ne++);
+    RG_CUDA(cudaEventRecord(done, st));
+    RG_CUDA(cudaStreamWaitEvent(cout, done, 0));
+    RG_CUDA(cudaMemcpyAsync(static_cast<char *>(dout.data) + c0 * plane_out,
+                            static_cast<char *>(bout.get()) + c0 * plane_out, size_t(cn * plane_out),
+                            cudaMemcpyDeviceToHost, cout));
+  }
+  cudaEvent_t fin = t_events.get(ne++);
+  RG_CUDA(cudaEventRecord(fin, cout));
+  RG_CUDA(cudaStreamWaitEvent(st, fin, 0));
+  join.dismiss();
+  RG_CUDA(cudaEventSynchronize(fin));
+}
+
+// ---- host arrays with a batch dimension: copy-in, compute and copy-out overlapped ----
+//
+// When the outermost dimension is not transformed, its slabs are independent transforms. A
+// host call then runs as a three-stage pipeline: slab i is copied in on the copy-in stream,
+// transformed on one of two compute streams as soon as it has arrived, and copied out on the
+// copy-out stream, while slab i+1 is copied in and slab i-1 copied out; the two link
+// directions run at once. Dense C-order host arrays only (every slab is one contiguous range
+// of both arrays), and only when the copies are large enough to matter.
+
+bool slabs_ok(const Desc &din, const Desc &dout, const std::vector<uint64_t> &ax) {
+  if (din.shape.empty() || din.shape[0] < 2 || dout.shape.empty() || dout.shape[0] != din.shape[0]) return false;
+  for (uint64_t a : ax)
+    if (a == 0) return false;
+  if (!din.data || !dout.data || !dense_c(din) || !dense_c(dout)) return false;
+  const int64_t bytes = din.shape[0] * din.bstride[0] + dout.shape[0] * dout.bstride[0];
+  if (bytes < (int64_t(2) << 20)) return false;
+  // pageable memory is copied through the driver's staging buffers, synchronously with the
+  // host: smaller copies only add overhead there (measured 310 us whole vs 499 us in 4 slabs
+  // for 256 x 4096 complex128)
+  return is_pinned_host(din.data) && is_pinned_host(dout.data);
+}
 
 template <class Body>
 void pipelined_slabs(const Desc &din, const Desc &dout, Body body) {
