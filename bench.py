@@ -294,6 +294,52 @@ def run_c1(args):
         print(json.dumps(line), flush=True)
 
 
+def cpu_c4(x_dev, W_dev, axes):
+    """The C4 step on the host cores with the reference's CPU algorithm (the oracle port, all
+    threads): r2c of the volume, the loss gradient 2|W|^2 X, and the adjoint (c2r with the
+    interior bins halved). One step, 64 + 64 transforms."""
+    import oracle
+
+    P = oracle.port()
+    cores = os.cpu_count() or 1
+    x = x_dev.detach().cpu().numpy()
+    w2 = (2 * W_dev.abs().square()).cpu().numpy()
+    X = np.empty(w2.shape, np.complex64)
+    g = np.empty_like(x)
+    P.r2c(x[:1], X[:1], list(axes), True, 1.0, cores)  # plans
+    t0 = time.perf_counter()
+    P.r2c(x, X, list(axes), True, 1.0, cores)
+    X *= w2
+    X[..., 1:-1] *= 0.5
+    P.c2r(X, g, list(axes), False, 1.0, cores)
+    dt = time.perf_counter() - t0
+    return {"value": 128 / dt, "unit": "transforms/s", "cores": cores, "kind": "port",
+            "sample": f"one step (64 r2c + 64 adjoint c2r of 1024^2, {dt:.2f} s), nthreads={cores}"}
+
+
+def cpu_c5(f_dev, shape):
+    """The float64-throughout Neumann solve on the host cores with the reference's CPU algorithm
+    (the oracle port, all threads): DCT-II over all axes, divide by the eigenvalues (constant mode
+    zero), DCT-III with fct 1/(8 n0 n1 n2). One solve."""
+    import oracle
+
+    P = oracle.port()
+    cores = os.cpu_count() or 1
+    f = f_dev.cpu().numpy()
+    lam = [2 * np.cos(np.pi * np.arange(n) / n) - 2 for n in shape]
+    F = np.empty_like(f)
+    u = np.empty_like(f)
+    t0 = time.perf_counter()
+    P.dct(f, F, [0, 1, 2], 2, 1.0, False, cores)
+    d = lam[0][:, None, None] + lam[1][None, :, None] + lam[2][None, None, :]
+    d[0, 0, 0] = np.inf
+    F /= d
+    P.dct(F, u, [0, 1, 2], 3, 1.0 / (8.0 * np.prod(shape)), False, cores)
+    dt = time.perf_counter() - t0
+    return {"value": 1 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"one float64 solve of 512^3 ({dt:.2f} s), nthreads={cores}"}
+
+
 def run_c4(args):
     """Config 4: differentiable rfftn float32 64 x 1024 x 1024 over axes (1, 2); loss =
     sum |W * rfftn(x)|^2; gradient by the adjoint kernel (c2r with halved interior bins)."""
@@ -343,11 +389,12 @@ def run_c4(args):
     e2e = {"value": e2e_rate(torch, args.steps, e2e_in, e2e_run, lambda: gh.copy_(xe.grad, non_blocking=True), 128),
            "unit": "transforms/s", "h2d_bytes_per_step": xh.numel() * 4, "d2h_bytes_per_step": gh.numel() * 4,
            "path": "torch_ops.rfftn forward + adjoint on a pinned host volume copied in, gradient copied out"}
+    cpu = cpu_c4(xs[0], W, axes) if rank == 0 and world == 1 else None
     line = base_line(METRIC, value, "transforms/s", world, args, ms, "f32",
                      {"workload": "rfftn float32 64 x 1024 x 1024 axes (1,2), loss sum|W*X|^2, forward + adjoint",
                       "global_batch": 64 * world, "l2": "2 rotating 256 MiB inputs > L2"})
     line.update({"roofline": roof, "kernels": kernels, "accuracy": {"grad_rel_l2_vs_torch_fp64": err},
-                 "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
+                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -410,7 +457,8 @@ def run_c5(args):
                               "plain_rel_residual": info_plain["rel_residual"],
                               "mixed_vs_plain_rel_l2": diff},
                  "fp64_plain_form": {"ms_per_solve": ms_plain, "solves_per_s": 1e3 / ms_plain},
-                 "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
+                 "cpu_baseline": cpu_c5(f, shape) if rank == 0 and world == 1 else None,
+                 "e2e": e2e, "gpu_launches": launches, "clocks": clocks})
     if rank == 0:
         print(json.dumps(line), flush=True)
 

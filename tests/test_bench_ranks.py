@@ -4,7 +4,8 @@ rendezvous on 127.0.0.1) run the same helpers the GPU bench runs under torchrun.
 Checked: `dist_init` reads WORLD_SIZE / RANK / LOCAL_RANK; `max_over_ranks` returns the
 slowest rank's time on every rank; `job_rate` counts the units of all ranks over that time;
 the reference arm (`run_reference`) does its work and prints on rank 0 only, so a rank other
-than 0 returns at once with nothing on stdout. No GPU is used."""
+than 0 returns at once with nothing on stdout. Also the C4 / C5 CPU-baseline helpers on small
+stand-ins. No GPU is used."""
 
 from __future__ import annotations
 
@@ -87,3 +88,40 @@ def test_single_process_helpers():
 
     assert bench.max_over_ranks(None, 3.5, 1, "cpu") == 3.5  # no process group needed
     assert bench.job_rate(1, 256, 10, 1000.0) == pytest.approx(2560.0)
+
+
+def test_cpu_baselines_compute_the_workload():
+    """The C4 / C5 CPU baselines (oracle port on the host cores) on small stand-ins: the Poisson
+    baseline's solution satisfies the 7-point Neumann system, the C4 step runs; both report a
+    positive rate with their core count."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    x = torch.randn(4, 64, 64)
+    W = torch.complex(torch.randn(4, 64, 33), torch.randn(4, 64, 33))
+    c4 = bench.cpu_c4(x, W, (1, 2))
+    assert c4["value"] > 0 and c4["cores"] >= 1 and c4["kind"] == "port"
+    n = 24
+    f = torch.randn(n, n, n, dtype=torch.float64)
+    f -= f.mean()
+    c5 = bench.cpu_c5(f, (n, n, n))
+    assert c5["value"] > 0
+    # the same solve, checked against the stencil
+    import oracle
+
+    P = oracle.port()
+    fn = f.numpy()
+    lam = [2 * np.cos(np.pi * np.arange(n) / n) - 2] * 3
+    F, u = np.empty_like(fn), np.empty_like(fn)
+    P.dct(fn, F, [0, 1, 2], 2, 1.0, False, 1)
+    d = lam[0][:, None, None] + lam[1][None, :, None] + lam[2][None, None, :]
+    d[0, 0, 0] = np.inf
+    F /= d
+    P.dct(F, u, [0, 1, 2], 3, 1.0 / (8.0 * n**3), False, 1)
+    up = np.pad(u, 1, mode="edge")
+    Au = (up[2:, 1:-1, 1:-1] + up[:-2, 1:-1, 1:-1] + up[1:-1, 2:, 1:-1] + up[1:-1, :-2, 1:-1]
+          + up[1:-1, 1:-1, 2:] + up[1:-1, 1:-1, :-2] - 6 * u)
+    assert np.linalg.norm(Au - fn) / np.linalg.norm(fn) < 1e-12
