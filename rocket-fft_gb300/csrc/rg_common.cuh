@@ -83,6 +83,41 @@ enum Op : int {
   OP_COUNT = 17
 };
 
+constexpr int kFlagStream = 4;
+
+// L2 cache policy for a launch's input loads: evict-first when the launch reads its input once
+// (kFlagStream), so that it does not push out of L2 the data the next launch reads; evict-normal
+// otherwise. One policy register per thread, one load instruction for both cases.
+__device__ __forceinline__ uint64_t input_policy(bool once) {
+  uint64_t pol;
+  if (once)
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  else
+    asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+// Read-only global loads with an L2 cache policy.
+__device__ __forceinline__ float ld_in(const float *p, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_in(const double *p, uint64_t pol) {
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float2 ld_in(const float2 *p, uint64_t pol) {
+  float2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ld_in(const double2 *p, uint64_t pol) {
+  double2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+
 struct KArgs {
   const void *in;
   void *out;
@@ -95,7 +130,8 @@ struct KArgs {
   int ps;          // pad shift: shared index i is stored at i + (i >> ps)
   int conj_in;     // conjugate while loading (backward transforms run the forward core on
   int conj_out;    // conjugated data) / while storing
-  int flags;       // op-specific: bit 1 = sine transform (DST) for the fused DCT ops
+  int flags;       // bit 1 (op-specific) = sine transform (DST) for the fused DCT ops; bit 2 =
+                   // the input is read once (out-of-place launch): loads evict-first (kFlagStream)
   double fct;      // scale applied to every output
   double bscale;   // r2c/c2r: extra scale of the interior half-spectrum bins 0 < k < n/2 (1 for
                    // the transforms; 2 / 0.5 for the adjoints of c2r / r2c)

@@ -143,22 +143,23 @@ __device__ __forceinline__ void fx_compute(const KArgs &a, uint32_t row0, int r,
   if constexpr (SRC == FX_GLOBAL) {
     const int64_t s = a.ld.axis_stride;
     const int64_t off = side_offset32(a.ld, row0 + uint32_t(r));
+    const uint64_t once = input_policy((a.flags & kFlagStream) != 0);
     if constexpr (OP == OP_R2C_EVEN) {
       const T *in = reinterpret_cast<const T *>(a.in) + off;
       if (pair_ok) {
         const cx<T> *p = reinterpret_cast<const cx<T> *>(in) + j;
 #pragma unroll
-        for (int k = 0; k < R; ++k) v[k] = __ldg(p + k * LR);
+        for (int k = 0; k < R; ++k) v[k] = ld_in(p + k * LR, once);
       } else {
         const T *p = in + 2 * int64_t(j) * s;
 #pragma unroll
-        for (int k = 0; k < R; ++k) v[k] = mk<T>(__ldg(p + 2 * k * LR * s), __ldg(p + (2 * k * LR + 1) * s));
+        for (int k = 0; k < R; ++k) v[k] = mk<T>(ld_in(p + 2 * k * LR * s, once), ld_in(p + (2 * k * LR + 1) * s, once));
       }
     } else {
       const cx<T> *p = reinterpret_cast<const cx<T> *>(a.in) + off + int64_t(j) * s;
       const int64_t step = int64_t(LR) * s;
 #pragma unroll
-      for (int k = 0; k < R; ++k) v[k] = __ldg(p + k * step);
+      for (int k = 0; k < R; ++k) v[k] = ld_in(p + k * step, once);
       if constexpr (BWD) {
 #pragma unroll
         for (int k = 0; k < R; ++k) v[k] = mk<T>(v[k].y, v[k].x);
@@ -485,6 +486,7 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
   // staged loops: thread -> (row, first element), TPR threads per row
   const int sr = COL ? (tid & (TB - 1)) : tid / TPR;
   const int si0 = COL ? tid / TB : tid % TPR;
+  const uint64_t once = input_policy((a.flags & kFlagStream) != 0);
 
   if constexpr (OP == OP_C2C) {
     if constexpr (NP == 1) {
@@ -560,8 +562,8 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
         for (int q = 0; q < NQ; ++q) {
           const int m = si0 + q * TPR;
           if (HP % TPR == 0 || m < HP) {
-            if (pair_ok) xv[q] = __ldg(reinterpret_cast<const cx<T> *>(p) + m);
-            else xv[q] = mk<T>(__ldg(p + 2 * m * s), __ldg(p + (2 * m + 1) * s));
+            if (pair_ok) xv[q] = ld_in(reinterpret_cast<const cx<T> *>(p) + m, once);
+            else xv[q] = mk<T>(ld_in(p + 2 * m * s, once), ld_in(p + (2 * m + 1) * s, once));
           }
         }
         cx<T> *row = buf + sr * PITCH;
@@ -589,8 +591,8 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
           const int i = si0 + q * TPR;
           if (L % TPR == 0 || i < L) {
             const int sa = sine ? L - 1 - i : i;
-            const T xa = __ldg(p + sa * s);
-            const T xb = i == 0 ? T(0) : __ldg(p + (sine ? i - 1 : L - i) * s);
+            const T xa = ld_in(p + sa * s, once);
+            const T xb = i == 0 ? T(0) : ld_in(p + (sine ? i - 1 : L - i) * s, once);
             xv[q] = mk<T>(xa, xb);
           }
         }
@@ -628,8 +630,8 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
         for (int q = 0; q < NQ; ++q) {
           const int m = si0 + q * TPR;
           if (HP % TPR == 0 || m < HP) {
-            if (pair_ok) xv[q] = __ldg(reinterpret_cast<const cx<T> *>(p) + m);
-            else xv[q] = mk<T>(__ldg(p + 2 * m * s), __ldg(p + (2 * m + 1) * s));
+            if (pair_ok) xv[q] = ld_in(reinterpret_cast<const cx<T> *>(p) + m, once);
+            else xv[q] = mk<T>(ld_in(p + 2 * m * s, once), ld_in(p + (2 * m + 1) * s, once));
           }
         }
         T *row = reinterpret_cast<T *>(buf + sr * PITCH);
@@ -713,7 +715,7 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
       auto xdd = [&](int q) -> T {  // x''_q
         if (q >= N) return T(0);
         const int src = sine ? N - 1 - q : q;
-        T v = __ldg(p + src * s);
+        T v = ld_in(p + src * s, once);
         if (src == 0) v *= e0;
         return v;
       };
@@ -764,8 +766,8 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
       for (int q = 0; q < NQ; ++q) {
         const int i = si0 + q * TPR;
         if (HP % TPR == 0 || i < HP) {
-          xa[q] = __ldg(p + i * s);
-          xb[q] = __ldg(p + (L - i) * s);
+          xa[q] = ld_in(p + i * s, once);
+          xb[q] = ld_in(p + (L - i) * s, once);
         }
       }
       auto fix = [&](int i, cx<T> x) {
