@@ -232,7 +232,6 @@ cudaStream_t side_stream(int which) {
   if (!s) RG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   return s;
 }
-cudaStream_t copy_stream() { return side_stream(kCopyIn); }
 
 // Slab count limit of the host-array pipelines: ROCKET_GPU_SLABS (0 = whole-array staging
 // always), default 4.
