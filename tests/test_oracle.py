@@ -172,3 +172,35 @@ def test_port_against_fftw_dct_dst(P, prec, fname):
         assert e <= (1e-5 if prec == "f32" else 1e-12), (key, e)
         checked += 1
     assert checked > 0
+
+
+def _child_transform(q):
+    import numpy as np
+
+    import oracle as o
+
+    z = np.random.default_rng(5).standard_normal((64, 256)) + 0j
+    out = np.empty_like(z)
+    o.port().c2c(z, out, [1], True, 1.0, 4)
+    q.put(float(np.abs(out - np.fft.fft(z, axis=1)).max()))
+
+
+@pytest.mark.filterwarnings("ignore:This process .* is multi-threaded:DeprecationWarning")
+def test_port_workers_after_fork(P):
+    """The port's persistent worker threads do not exist in a forked child: a child process
+    that forks after the parent used them builds its own and finishes its threaded transform."""
+    import multiprocessing as mp
+
+    z = np.random.default_rng(6).standard_normal((64, 256)) + 0j
+    P.c2c(z, np.empty_like(z), [1], True, 1.0, 4)  # the parent's workers exist now
+    ctx = mp.get_context("fork")
+    q = ctx.Queue()
+    p = ctx.Process(target=_child_transform, args=(q,))
+    p.start()
+    p.join(timeout=60)
+    if p.is_alive():
+        p.kill()
+        p.join()
+        pytest.fail("forked child did not finish its transform")
+    assert p.exitcode == 0
+    assert q.get(timeout=5) < 1e-9
