@@ -175,15 +175,13 @@ class Staged {
   void alias(const Staged &o) {
     view_.data = o.view_.data;
     buf_.reset();
-    shared_ = true;
   }
-  bool shared() const { return shared_; }
 
  private:
   Desc d_;
   cudaStream_t st_;
   NdArray view_;
-  bool device_ = false, shared_ = false;
+  bool device_ = false;
   int64_t span_lo_ = 0;
   size_t span_ = 0;
   std::unique_ptr<rg::DevBuf> buf_;
