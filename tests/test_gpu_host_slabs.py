@@ -4,7 +4,8 @@ overlapped) once the copies pass 2 MiB. Every transform family goes through it h
 the oracle: c2c (out of place and in place), r2c / c2r (forward and backward flags), c2c_sym,
 DCT / DST (types 1-4, ortho), FFTPACK r2r and both Hartley forms, with slab counts that do not
 divide the outer extent, four-dimensional arrays and several host threads at once; pageable
-arrays and a call below the size threshold take whole-array staging and are checked too.
+arrays, a call below the size threshold and reversed views (negative strides) take whole-array
+staging and are checked too.
 Tolerance: relative L2 <= 1e-6 (single), <= 1e-13 (double) against the oracle's double result."""
 
 from __future__ import annotations
@@ -148,3 +149,38 @@ def test_slabs_from_threads(rg, cuda):
         outs = list(ex.map(work, range(len(xs))))
     for x, y in zip(xs, outs):
         assert oracle.rel_l2(y, np.fft.fft(x, axis=1)) <= 1e-13
+
+
+@pytest.mark.parametrize("cdt", [np.complex64, np.complex128])
+def test_negative_strides(rg, cuda, cdt):
+    """Reversed NumPy views (negative byte strides) in and out, which the reference accepts:
+    staged through the GPU as the address span they cover, strides kept."""
+    rng = np.random.default_rng(36)
+    rdt = np.float32 if cdt == np.complex64 else np.float64
+    tol = TOL[np.dtype(cdt)]
+    P = oracle.port()
+    zb = _cplx(rng, (24, 96), cdt)
+    z = zb[::-1, ::-2]
+    for axes in ([1], [0], [0, 1]):
+        want = np.empty(z.shape, np.complex128)
+        P.c2c(z.astype(np.complex128), want, axes, True, 0.5, 4)
+        out = np.empty_like(zb)[::-1, ::-2]
+        rg.c2c(z, out, np.array(axes), True, 0.5, 1)
+        assert oracle.rel_l2(out, want) <= tol, axes
+    xb = rng.standard_normal((20, 64)).astype(rdt)
+    x = xb[::-1, ::-1]
+    want = np.empty((20, 33), np.complex128)
+    P.r2c(x.astype(np.float64), want, [0, 1], True, 1.0, 4)
+    X = np.empty((20, 33), cdt)[::-1]
+    rg.r2c(x, X, np.array([0, 1]), True, 1.0, 1)
+    assert oracle.rel_l2(X, want) <= tol, "r2c"
+    want_y = np.empty((20, 64))
+    P.c2r(X.astype(np.complex128), want_y, [0, 1], False, 1 / 1280, 4)
+    y = np.empty_like(xb)[:, ::-1]
+    rg.c2r(X, y, np.array([0, 1]), False, 1 / 1280, 1)
+    assert oracle.rel_l2(y, want_y) <= TOL[np.dtype(rdt)], "c2r"
+    want_d = np.empty((20, 64))
+    P.dct(x.astype(np.float64), want_d, [1], 2, 1.0, False, 4)
+    d = np.empty_like(xb)[::-1]
+    rg.dct(x, d, np.array([1]), 2, 1.0, False, 1)
+    assert oracle.rel_l2(d, want_d) <= TOL[np.dtype(rdt)], "dct"

@@ -204,3 +204,33 @@ def test_port_workers_after_fork(P):
         pytest.fail("forked child did not finish its transform")
     assert p.exitcode == 0
     assert q.get(timeout=5) < 1e-9
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference oracle not built on this host")
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_port_matches_reference_negative_strides(P, prec):
+    """Reversed and reversed-strided NumPy views (negative byte strides), in and out."""
+    R = oracle.ref()
+    rng = np.random.default_rng(77)
+    rdt, cdt = RDT[prec], {"f32": np.complex64, "f64": np.complex128}[prec]
+    tol = TOL[prec]
+    zb = (rng.standard_normal((12, 40)) + 1j * rng.standard_normal((12, 40))).astype(cdt)
+    z = zb[::-1, ::-2]
+    for axes in ([1], [0], [0, 1]):
+        a = np.empty_like(zb)[::-1, ::-2]
+        b = np.empty(z.shape, cdt)
+        P.c2c(z, a, axes, True, 1.0)
+        R.c2c(z, b, axes, True, 1.0)
+        assert oracle.rel_l2(a, b) <= tol, axes
+    xb = rng.standard_normal((10, 36)).astype(rdt)
+    x = xb[::-1, ::-1]
+    a = np.empty((10, 19), cdt)[::-1]
+    b = np.empty((10, 19), cdt)
+    P.r2c(x, a, [0, 1], True, 1.0)
+    R.r2c(x, b, [0, 1], True, 1.0)
+    assert oracle.rel_l2(a, b) <= tol, "r2c"
+    a = np.empty_like(xb)[:, ::-1]
+    b = np.empty_like(xb)
+    P.dct(x, a, [1], 2, 1.0, False)
+    R.dct(x, b, [1], 2, 1.0, False)
+    assert oracle.rel_l2(a, b) <= tol, "dct"
