@@ -184,6 +184,35 @@ template <class T> static C<T> unit(u64 t, u64 N) {  // e^{+2 pi i t/N}
   return {T(c), T(s)};
 }
 
+// e^{+2 pi i t / N} for many t < N at one N: two tables of about sqrt(N) roots each (by
+// root()), hi_j = e^{2 pi i j S / N} and lo_j = e^{2 pi i j / N}, S the power of two at or
+// above sqrt(N); a root is the double-precision product hi_{t / S} lo_{t mod S}, rounded once
+// to T. O(sqrt(N)) cos/sin calls instead of one per twiddle, as the reference's table method
+// (HDR:466-544).
+class Roots {
+ public:
+  explicit Roots(u64 N) : N_(N), shift_(0) {
+    while ((u64(1) << shift_) * (u64(1) << shift_) < N) ++shift_;
+    const u64 S = u64(1) << shift_;
+    for (u64 j = 0; j < S; ++j) lo_.push_back(dbl(j));
+    for (u64 j = 0; j * S < N; ++j) hi_.push_back(dbl(j * S));
+  }
+  template <class T> C<T> get(u64 t) const {
+    const C<double> a = hi_[t >> shift_], b = lo_[t & ((u64(1) << shift_) - 1)];
+    return {T(a.r * b.r - a.i * b.i), T(a.r * b.i + a.i * b.r)};
+  }
+
+ private:
+  C<double> dbl(u64 t) const {
+    double c, s;
+    root(t, N_, c, s);
+    return {c, s};
+  }
+  u64 N_;
+  int shift_;
+  std::vector<C<double>> lo_, hi_;
+};
+
 // ---------------------------------------------------------------------------------------
 // packed complex FFT (role of cfftp, HDR:1060-1830): Stockham passes
 // ---------------------------------------------------------------------------------------
@@ -216,9 +245,10 @@ template <class T> class CPack {
     u64 ns = 1;
     for (u64 R : fac_) {
       off_.push_back(tw_.size());
+      const Roots roots(ns * R);
       for (u64 k = 1; k < R; ++k)
-        for (u64 m = 0; m < ns; ++m) tw_.push_back(unit<T>(m * k, ns * R));  // e^{+}
-      if (generic(R)) {
+        for (u64 m = 0; m < ns; ++m) tw_.push_back(roots.get<T>(m * k));  // e^{+2 pi i m k / (ns R)}
+      if (!specialised(R)) {  // odd radices: the roots of unity of order R
         roots_off_.push_back(rt_.size());
         for (u64 t = 0; t < R; ++t) rt_.push_back(unit<T>(t, R));
       } else {
@@ -233,7 +263,8 @@ template <class T> class CPack {
   template <class D> void exec(C<D> *c, T fct, bool fwd) const { fwd ? run<true>(c, fct) : run<false>(c, fct); }
 
  private:
-  static bool generic(u64 R) { return R != 2 && R != 3 && R != 4 && R != 5 && R != 8; }
+  static bool specialised(u64 R) { return R == 2 || R == 3 || R == 4 || R == 5 || R == 8; }
+  static bool odd_unrolled(u64 R) { return R == 7 || R == 11 || R == 13; }
 
   template <bool FWD, class D> void run(C<D> *c, T fct) const {
     if (n_ == 1) {
@@ -250,13 +281,17 @@ template <class T> class CPack {
       C<D> *b = p + 1 == np && np > 1 ? c : (p % 2 == 0 ? s1 : s2);
       const u64 R = fac_[p];
       const C<T> *tw = tw_.data() + off_[p];
+      const C<T> *rt = rt_.data() + roots_off_[p];
       switch (R) {
         case 2: pass<FWD, 2>(ns, a, b, tw, [](C<D>(&v)[2]) { dft2(v); }); break;
         case 3: pass<FWD, 3>(ns, a, b, tw, [](C<D>(&v)[3]) { dft3<FWD>(v); }); break;
         case 4: pass<FWD, 4>(ns, a, b, tw, [](C<D>(&v)[4]) { dft4<FWD>(v); }); break;
         case 5: pass<FWD, 5>(ns, a, b, tw, [](C<D>(&v)[5]) { dft5<FWD>(v); }); break;
         case 8: pass<FWD, 8>(ns, a, b, tw, [](C<D>(&v)[8]) { dft8<FWD>(v); }); break;
-        default: passg<FWD>(R, ns, a, b, tw, rt_.data() + roots_off_[p]);
+        case 7: pass<FWD, 7>(ns, a, b, tw, [rt](C<D>(&v)[7]) { dft_odd<FWD, 7>(v, rt); }); break;
+        case 11: pass<FWD, 11>(ns, a, b, tw, [rt](C<D>(&v)[11]) { dft_odd<FWD, 11>(v, rt); }); break;
+        case 13: pass<FWD, 13>(ns, a, b, tw, [rt](C<D>(&v)[13]) { dft_odd<FWD, 13>(v, rt); }); break;
+        default: passg<FWD>(R, ns, a, b, tw, rt);
       }
       a = b;
       ns *= R;
@@ -389,6 +424,32 @@ template <class T> class CPack {
     }
   }
 
+  // odd radix R unrolled at compile time: the pairing of passg with R fixed (rt = the roots of
+  // order R); same operations in the same order, so the same results as the generic pass
+  template <bool FWD, int R, class D> static void dft_odd(C<D> (&v)[R], const C<T> *rt) {
+    constexpr int H = (R - 1) / 2;
+    C<D> sk[H + 1], dk[H + 1], out[R];
+    C<D> y0 = v[0];
+    for (int k = 1; k <= H; ++k) {
+      sk[k] = v[k] + v[R - k];
+      dk[k] = v[k] - v[R - k];
+      y0 = y0 + sk[k];
+    }
+    out[0] = y0;
+    for (int q = 1; q <= H; ++q) {
+      C<D> A = v[0], B = {D{}, D{}};
+      for (int k = 1; k <= H; ++k) {
+        const int e = (q * k) % R;
+        A = A + scale(sk[k], rt[e].r);
+        B = B + scale(dk[k], rt[e].i);
+      }
+      const C<D> iB = {-B.i, B.r};
+      out[q] = FWD ? A - iB : A + iB;
+      out[R - q] = FWD ? A + iB : A - iB;
+    }
+    for (int q = 0; q < R; ++q) v[q] = out[q];
+  }
+
   u64 n_;
   std::vector<u64> fac_;
   std::vector<size_t> off_, roots_off_;
@@ -404,11 +465,12 @@ template <class T> class Blue {
   explicit Blue(u64 n) : n_(n), n2_(good_size_cmplx(2 * n - 1)), plan_(n2_), bk_(n), bkf_(n2_) {
     // bk[m] = e^{+i pi m^2 / n}, the exponent accumulated modulo 2n (HDR:2773-2780)
     bk_[0] = {T(1), T(0)};
+    const Roots roots(2 * n);
     u64 coeff = 0;
     for (u64 m = 1; m < n; ++m) {
       coeff += 2 * m - 1;
       if (coeff >= 2 * n) coeff -= 2 * n;
-      bk_[m] = unit<T>(coeff, 2 * n);
+      bk_[m] = roots.get<T>(coeff);
     }
     // zero-padded, symmetric, normalised, transformed (HDR:2783-2792)
     std::vector<C<T>> t(n2_, C<T>{T(0), T(0)});
@@ -479,7 +541,8 @@ template <class T> class RPlan {
     if (n == 0) throw std::runtime_error("zero-length FFT requested");
     if (n % 2 == 0 && !use_bluestein(n, 0.5)) {
       half_.reset(new CPlan<T>(n / 2));
-      for (u64 k = 0; k <= n / 2; ++k) w_.push_back(unit<T>(k, n));  // e^{+2 pi i k/n}
+      const Roots roots(n);
+      for (u64 k = 0; k <= n / 2; ++k) w_.push_back(roots.get<T>(k));  // e^{+2 pi i k/n}
     } else {
       full_.reset(new CPlan<T>(n));
     }
@@ -628,7 +691,8 @@ template <class T> class Dst1 {  // HDR:2957-2985: rfft of the odd extension, le
 template <class T> class Dcst23 {  // HDR:2987-3061
  public:
   explicit Dcst23(u64 n) : fft_(n), tw_(n) {
-    for (u64 i = 0; i < n; ++i) tw_[i] = unit<T>(i + 1, 4 * n).r;  // cos(2 pi (i+1) / 4n)
+    const Roots roots(4 * n);
+    for (u64 i = 0; i < n; ++i) tw_[i] = roots.get<T>(i + 1).r;  // cos(2 pi (i+1) / 4n)
   }
   u64 length() const { return fft_.length(); }
   template <class D> void exec(D *c, T fct, bool ortho, int type, bool cosine) const {
@@ -688,7 +752,8 @@ template <class T> class Dcst4 {  // HDR:3063-3163
       rfft_.reset(new RPlan<T>(n));
     } else {
       fft_.reset(new CPlan<T>(n / 2));
-      for (u64 i = 0; i < n / 2; ++i) C2_.push_back(conj(unit<T>(8 * i + 1, 16 * n)));
+      const Roots roots(16 * n);
+      for (u64 i = 0; i < n / 2; ++i) C2_.push_back(conj(roots.get<T>(8 * i + 1)));
     }
   }
   u64 length() const { return N_; }
