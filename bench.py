@@ -787,16 +787,79 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_sweep(args):
+    """Batched 1-D complex64 c2c and float32 r2c over lengths 2^10 .. 2^24 (forward, fct 1), each
+    length a batch of about 256 MiB of input (larger than L2) resident on the device: device
+    time per call with CUDA events (median of `steps` calls after `warmup`), algorithmic bytes
+    = input read + output written, as a fraction of the HBM peak. One JSON line; `value` is the
+    lowest c2c fraction over the lengths."""
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    rg = load_package()
+    peak, peak_kind = peaks()
+    gen = torch.Generator(device="cuda").manual_seed(17 + rank)
+    axes = np.array([1], dtype=np.int64)
+    reps, warm = max(3, min(args.steps, 20)), max(1, min(args.warmup, 3))
+
+    def timed(fn):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            out.append(a.elapsed_time(b))
+        return sorted(out)[len(out) // 2]
+
+    rows = []
+    with ClockSampler(local) as clk:
+        for e in range(10, 25):
+            L = 1 << e
+            B = max(1, (1 << 25) // L)  # 2^25 complex64 = 256 MiB per side
+            x = torch.complex(torch.randn((B, L), device="cuda", generator=gen),
+                              torch.randn((B, L), device="cuda", generator=gen))
+            y = torch.empty_like(x)
+            ms = timed(lambda: rg.c2c(x, y, axes, True, 1.0, 1))
+            c2c_bytes = 2 * B * L * 8
+            del x, y
+            Br = max(1, (1 << 26) // L)  # 2^26 float32 = 256 MiB of input
+            r = torch.randn((Br, L), device="cuda", generator=gen)
+            R = torch.empty((Br, L // 2 + 1), dtype=torch.complex64, device="cuda")
+            ms_r = timed(lambda: rg.r2c(r, R, axes, True, 1.0, 1))
+            r2c_bytes = Br * L * 4 + Br * (L // 2 + 1) * 8
+            del r, R
+            rows.append({"log2_length": e, "c2c_batch": B, "c2c_ms": ms, "c2c_gbs": c2c_bytes / (ms / 1e3) / 1e9,
+                         "c2c_frac": c2c_bytes / (ms / 1e3) / 1e9 / peak, "r2c_batch": Br, "r2c_ms": ms_r,
+                         "r2c_gbs": r2c_bytes / (ms_r / 1e3) / 1e9,
+                         "r2c_frac": r2c_bytes / (ms_r / 1e3) / 1e9 / peak})
+    if rank == 0:
+        line = {"metric": "fraction of HBM peak, batched complex64 c2c over lengths 2^10..2^24 (lowest)",
+                "value": min(r["c2c_frac"] for r in rows), "unit": "fraction", "n_gpus": world,
+                "steps": reps, "warmup": warm, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded N(0,1))",
+                "config": {"workload": "batched 1-D c2c complex64 and r2c float32, lengths 2^10..2^24, "
+                                       "about 256 MiB of input per length", "l2": "256 MiB inputs > L2"},
+                "peak": peak, "peak_source": peak_kind, "rows": rows, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "sweep"],
                     help="c2 (default): the float32 256^3 r2c + c2r round trip; c1: complex128 c2c "
                          "256 x 4096; c3: 10,000 uneven complex64 lengths in one launch; c4: "
-                         "differentiable rfftn 64 x 1024^2; c5: Neumann Poisson 512^3")
+                         "differentiable rfftn 64 x 1024^2; c5: Neumann Poisson 512^3; sweep: batched "
+                         "complex64 c2c / float32 r2c over lengths 2^10..2^24 against the HBM peak")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -808,6 +871,8 @@ def main():
         run_c4(args)
     elif args.config == "c5":
         run_c5(args)
+    elif args.config == "sweep":
+        run_sweep(args)
     else:
         run_ours(args)
 
