@@ -59,10 +59,17 @@ def load_package():
 
 
 def peaks():
+    """HBM copy bandwidth (GB/s) for the roofline: the measured figure of this machine's GPUs
+    when MEASURED_PEAKS.json holds one, else the 6,800 GB/s fallback (one earlier GB300
+    measurement). Returns (GB/s, "measured" | "fallback")."""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
-        d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
+        try:
+            v = float(json.loads(p.read_text())["hbm_gbs"])
+            if v > 0:
+                return v, "measured"
+        except (ValueError, KeyError, TypeError):
+            pass
     return 6800.0, "fallback"
 
 

@@ -125,3 +125,19 @@ def test_cpu_baselines_compute_the_workload():
     Au = (up[2:, 1:-1, 1:-1] + up[:-2, 1:-1, 1:-1] + up[1:-1, 2:, 1:-1] + up[1:-1, :-2, 1:-1]
           + up[1:-1, 1:-1, 2:] + up[1:-1, 1:-1, :-2] - 6 * u)
     assert np.linalg.norm(Au - fn) / np.linalg.norm(fn) < 1e-12
+
+
+def test_peaks_file_handling(tmp_path, monkeypatch):
+    """The roofline peak: the measured copy bandwidth from MEASURED_PEAKS.json when the file
+    holds a positive `hbm_gbs`, else the fallback (missing file, missing key, bad value)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    assert bench.peaks() == (6800.0, "fallback")
+    (tmp_path / "MEASURED_PEAKS.json").write_text('{"hbm_gbs": 6663.9, "bf16_tflops": 1900}')
+    assert bench.peaks() == (6663.9, "measured")
+    (tmp_path / "MEASURED_PEAKS.json").write_text('{"bf16_tflops": 1900}')
+    assert bench.peaks() == (6800.0, "fallback")
+    (tmp_path / "MEASURED_PEAKS.json").write_text('{"hbm_gbs": "n/a"}')
+    assert bench.peaks() == (6800.0, "fallback")
