@@ -729,6 +729,20 @@ def run_ours(args):
         finally:
             rg.set_tc_split(prev)
 
+    # the length range 2^10 .. 2^24: batched complex64 c2c and float32 r2c, fraction of the peak
+    # per length (one call per length and kind, 256 MiB of input, median of 5 after 2 warm-ups)
+    length_range = None
+    if rank == 0:
+        rows = sweep_rows(torch, rg, torch.Generator(device=dev).manual_seed(17), peak, 5, 2)
+        length_range = {
+            "what": "batched 1-D complex64 c2c and float32 r2c, one length 2^e per row, about 256 MiB of "
+                    "input per call, device time (median of 5), algorithmic bytes = input read + output written",
+            "peak": peak, "peak_source": peak_kind,
+            "min_c2c_frac": min(r["c2c_frac"] for r in rows), "min_r2c_frac": min(r["r2c_frac"] for r in rows),
+            "rows": [{"log2_length": r["log2_length"], "c2c_ms": round(r["c2c_ms"], 4),
+                      "c2c_frac": round(r["c2c_frac"], 3), "r2c_ms": round(r["r2c_ms"], 4),
+                      "r2c_frac": round(r["r2c_frac"], 3)} for r in rows]}
+
     # e2e: the same round trip through the C ABI on pinned host arrays
     e2e = None
     if rank == 0:
@@ -784,6 +798,7 @@ def run_ours(args):
             "forms": {"plain_fp32": {"value": value, "ms_per_step": ms / args.steps,
                                      "r2c_rel_l2_vs_fp64": acc.get("r2c_rel_l2_vs_fp64")},
                       "tc_split_fp16": tc_form},
+            "length_range": length_range,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,
@@ -794,21 +809,12 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def run_sweep(args):
-    """Batched 1-D complex64 c2c and float32 r2c over lengths 2^10 .. 2^24 (forward, fct 1), each
-    length a batch of about 256 MiB of input (larger than L2) resident on the device: device
-    time per call with CUDA events (median of `steps` calls after `warmup`), algorithmic bytes
-    = input read + output written, as a fraction of the HBM peak. One JSON line; `value` is the
-    lowest c2c fraction over the lengths."""
-    import torch
-
-    world, rank, local = dist_init()
-    torch.cuda.set_device(local)
-    rg = load_package()
-    peak, peak_kind = peaks()
-    gen = torch.Generator(device="cuda").manual_seed(17 + rank)
+def sweep_rows(torch, rg, gen, peak, reps, warm, exps=range(10, 25)):
+    """Per power-of-two length 2^e: a batch of about 256 MiB of complex64 input through c2c and of
+    float32 input through r2c (forward, fct 1), resident on the device; median device time of
+    `reps` calls after `warm` (CUDA events on the current stream), algorithmic bytes (input read +
+    output written) over that time, as a fraction of `peak` GB/s."""
     axes = np.array([1], dtype=np.int64)
-    reps, warm = max(3, min(args.steps, 20)), max(1, min(args.warmup, 3))
 
     def timed(fn):
         for _ in range(warm):
@@ -825,26 +831,44 @@ def run_sweep(args):
         return sorted(out)[len(out) // 2]
 
     rows = []
+    for e in exps:
+        L = 1 << e
+        B = max(1, (1 << 25) // L)  # 2^25 complex64 = 256 MiB per side
+        x = torch.complex(torch.randn((B, L), device="cuda", generator=gen),
+                          torch.randn((B, L), device="cuda", generator=gen))
+        y = torch.empty_like(x)
+        ms = timed(lambda: rg.c2c(x, y, axes, True, 1.0, 1))
+        c2c_bytes = 2 * B * L * 8
+        del x, y
+        Br = max(1, (1 << 26) // L)  # 2^26 float32 = 256 MiB of input
+        r = torch.randn((Br, L), device="cuda", generator=gen)
+        R = torch.empty((Br, L // 2 + 1), dtype=torch.complex64, device="cuda")
+        ms_r = timed(lambda: rg.r2c(r, R, axes, True, 1.0, 1))
+        r2c_bytes = Br * L * 4 + Br * (L // 2 + 1) * 8
+        del r, R
+        rows.append({"log2_length": e, "c2c_batch": B, "c2c_ms": ms, "c2c_gbs": c2c_bytes / (ms / 1e3) / 1e9,
+                     "c2c_frac": c2c_bytes / (ms / 1e3) / 1e9 / peak, "r2c_batch": Br, "r2c_ms": ms_r,
+                     "r2c_gbs": r2c_bytes / (ms_r / 1e3) / 1e9,
+                     "r2c_frac": r2c_bytes / (ms_r / 1e3) / 1e9 / peak})
+    return rows
+
+
+def run_sweep(args):
+    """Batched 1-D complex64 c2c and float32 r2c over lengths 2^10 .. 2^24 (forward, fct 1), each
+    length a batch of about 256 MiB of input (larger than L2) resident on the device: device
+    time per call with CUDA events (median of `steps` calls after `warmup`), algorithmic bytes
+    = input read + output written, as a fraction of the HBM peak. One JSON line; `value` is the
+    lowest c2c fraction over the lengths."""
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    rg = load_package()
+    peak, peak_kind = peaks()
+    gen = torch.Generator(device="cuda").manual_seed(17 + rank)
+    reps, warm = max(3, min(args.steps, 20)), max(1, min(args.warmup, 3))
     with ClockSampler(local) as clk:
-        for e in range(10, 25):
-            L = 1 << e
-            B = max(1, (1 << 25) // L)  # 2^25 complex64 = 256 MiB per side
-            x = torch.complex(torch.randn((B, L), device="cuda", generator=gen),
-                              torch.randn((B, L), device="cuda", generator=gen))
-            y = torch.empty_like(x)
-            ms = timed(lambda: rg.c2c(x, y, axes, True, 1.0, 1))
-            c2c_bytes = 2 * B * L * 8
-            del x, y
-            Br = max(1, (1 << 26) // L)  # 2^26 float32 = 256 MiB of input
-            r = torch.randn((Br, L), device="cuda", generator=gen)
-            R = torch.empty((Br, L // 2 + 1), dtype=torch.complex64, device="cuda")
-            ms_r = timed(lambda: rg.r2c(r, R, axes, True, 1.0, 1))
-            r2c_bytes = Br * L * 4 + Br * (L // 2 + 1) * 8
-            del r, R
-            rows.append({"log2_length": e, "c2c_batch": B, "c2c_ms": ms, "c2c_gbs": c2c_bytes / (ms / 1e3) / 1e9,
-                         "c2c_frac": c2c_bytes / (ms / 1e3) / 1e9 / peak, "r2c_batch": Br, "r2c_ms": ms_r,
-                         "r2c_gbs": r2c_bytes / (ms_r / 1e3) / 1e9,
-                         "r2c_frac": r2c_bytes / (ms_r / 1e3) / 1e9 / peak})
+        rows = sweep_rows(torch, rg, gen, peak, reps, warm)
     if rank == 0:
         line = {"metric": "fraction of HBM peak, batched complex64 c2c over lengths 2^10..2^24 (lowest)",
                 "value": min(r["c2c_frac"] for r in rows), "unit": "fraction", "n_gpus": world,

@@ -251,6 +251,13 @@ int rocketgpu_c2c_noalloc(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocke
 int rocketgpu_set_tc_split(int on);
 int rocketgpu_tc_error(void *stream);
 
+/* Long power-of-two complex64 transforms (2^14 .. 2^24 points; no reference counterpart: the
+ * reference runs such rows through cfftp::pass_all, rocket_fft/_pocketfft_hdronly.h:1690-1740)
+ * run as one persistent launch whose CTAs wait on each other's tiles, each wait bounded to 2 s.
+ * rocketgpu_long_error returns 1 if such a wait gave up since the previous call (and clears the
+ * flag), 0 otherwise, a negative status on failure. Synchronises `stream`. */
+int rocketgpu_long_error(void *stream);
+
 /* Two-axis plane kernels (no reference counterpart; off unless switched on here or by
  * ROCKET_GPU_PLANE=1). While on, an r2c over two or more axes whose last axis (contiguous, even
  * power-of-two length) and the axis before it fit one of the compiled plane sizes runs those

@@ -34,6 +34,7 @@ from .pocketfft import (  # noqa: F401
     set_tc_split,
     set_plane_kernels,
     tc_error,
+    long_error,
     tc_selftest,
     version,
 )

@@ -835,6 +835,12 @@ RG_EXPORT int rocketgpu_tc_error(void *stream) {
   return st == RG_OK ? flag : -st;
 }
 
+RG_EXPORT int rocketgpu_long_error(void *stream) {
+  int flag = 0;
+  const int st = guarded([&] { flag = rg::long_error_flag(static_cast<cudaStream_t>(stream)); });
+  return st == RG_OK ? flag : -st;
+}
+
 RG_EXPORT int rocketgpu_tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D,
                                     void *stream) {
   return guarded([&] {

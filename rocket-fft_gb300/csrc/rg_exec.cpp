@@ -331,7 +331,7 @@ bool fixed_job_ok(const Job &j) {
   if (ld.colmap != sd.colmap || j.nrows >= (int64_t(1) << 31)) return false;
   if (!set_fastdivs(ld) || !set_fastdivs(sd)) return false;
   if (j.op == OP_C2C && j.cin != j.cout) return false;
-  return j.L <= (ld.colmap ? 1024 : 4096);
+  return j.L <= (ld.colmap ? 1024 : 8192);
 }
 
 void run_job(const Job &j, cudaStream_t st) {
@@ -541,6 +541,10 @@ void c2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     run_job(j, st);
     return;
   }
+  if (long_c2c_ok(dt, n, in, ld, out, sd)) {
+    long_c2c(dt, n, in, ld, out, sd, nrows, cin, cout, fct, st);
+    return;
+  }
   int64_t n1, n2;
   if (core_smooth(uint64_t(n)) && four_step_split(dt, n, n1, n2)) {
     c2c_four_step(dt, n, n1, n2, in, ld, out, sd, nrows, cin, cout, fct, st);
@@ -618,6 +622,10 @@ void r2c_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     run_job(j, st);
     return;
   }
+  if (long_real_ok(dt, n, in, ld, sd, bscale)) {
+    long_r2c(n, in, ld, out, sd, nrows, cout, fct, st);
+    return;
+  }
   // general length: full complex transform of the real row, keep bins 0..n/2
   DevBuf ws(size_t(nrows) * size_t(n) * cx_size(dt), st);
   const Side w = contiguous_rows(nrows, n);
@@ -672,6 +680,10 @@ void c2r_rows(DType dt, int64_t n, const void *in, const Side &ld, void *out, co
     j.cout = false;
     j.fct = fct;
     run_job(j, st);
+    return;
+  }
+  if (long_real_ok(dt, n, out, sd, ld, bscale)) {
+    long_c2r(n, in, ld, out, sd, nrows, cin, fct, st);
     return;
   }
   DevBuf ws(size_t(nrows) * size_t(n) * cx_size(dt), st);

@@ -1,4 +1,4 @@
-// Launchers of the compile-time-L kernels (rg_fixed_kernel.cuh) for L = 64 ... 4096 (row walk)
+// Launchers of the compile-time-L kernels (rg_fixed_kernel.cuh) for L = 64 ... 8192 (row walk)
 // and L = 64 ... 1024 (column walk); instantiated per precision and op family in
 // rg_fixed_{f32,f64}{,_real,_dct}.cu.
 #pragma once
@@ -32,6 +32,7 @@ bool fx_by_length(int E, const KArgs &a, int pair_ok, cudaStream_t st) {
     switch (E) {
       case 11: fx_launch<T, OP, 11, COL, BWD>(a, pair_ok, st); return true;
       case 12: fx_launch<T, OP, 12, COL, BWD>(a, pair_ok, st); return true;
+      case 13: fx_launch<T, OP, 13, COL, BWD>(a, pair_ok, st); return true;
       default: break;
     }
   }

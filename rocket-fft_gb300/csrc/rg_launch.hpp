@@ -88,6 +88,20 @@ bool launch_tc_c2c(const KArgs &a, bool col, bool bwd, cudaStream_t st);
 int tc_error_flag(cudaStream_t st);
 void tc_selftest(const void *A, const void *A2, const void *B, const void *B2, float *D, cudaStream_t st);
 
+// Long power-of-two complex64 transforms, 2^14 .. 2^24 points (rg_long.cu): true when a batch of
+// rows with these sides can take the two-phase persistent kernel.
+bool long_c2c_ok(DType dt, int64_t n, const void *in, const Side &ld, const void *out, const Side &sd);
+void long_c2c(DType dt, int64_t n, const void *in, const Side &ld, void *out, const Side &sd, int64_t nrows,
+              bool cin, bool cout, double fct, cudaStream_t st);
+// float32 real rows of n = 2m points, m = 2^14 .. 2^23, through the same kernel on the real pairs.
+bool long_real_ok(DType dt, int64_t n, const void *real, const Side &rs, const Side &cs, double bscale);
+void long_r2c(int64_t n, const void *in, const Side &ld, void *out, const Side &sd, int64_t nrows, bool cout,
+              double fct, cudaStream_t st);
+void long_c2r(int64_t n, const void *in, const Side &ld, void *out, const Side &sd, int64_t nrows, bool cin,
+              double fct, cudaStream_t st);
+// 1 if a long-transform kernel gave up waiting on another CTA since the last call (cleared).
+int long_error_flag(cudaStream_t st);
+
 uint64_t launch_count();
 void note_launch();
 

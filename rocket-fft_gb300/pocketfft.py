@@ -429,6 +429,15 @@ def set_plane_kernels(on=True):
     return bool(_lib.load().rocketgpu_set_plane_kernels(1 if on else 0))
 
 
+def long_error(stream=None):
+    """1 if a long-transform kernel gave up waiting on another of its tiles since the previous
+    call (the flag is cleared), else 0."""
+    r = int(_lib.load().rocketgpu_long_error(ctypes.c_void_p(_stream_int(stream)) if stream else None))
+    if r < 0:
+        _raise_status(-r, "rocketgpu_long_error")
+    return r
+
+
 def tc_error(stream=None):
     """1 if a tensor-core kernel gave up waiting for its matrix products since load, else 0."""
     r = int(_lib.load().rocketgpu_tc_error(ctypes.c_void_p(_stream_int(stream)) if stream else None))

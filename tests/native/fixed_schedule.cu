@@ -20,7 +20,7 @@ template <typename T, int OP, int E, bool COL> int check_cfg() {
 template <typename T, int OP, bool COL> int check_all() {
   int bad = check_cfg<T, OP, 6, COL>() + check_cfg<T, OP, 7, COL>() + check_cfg<T, OP, 8, COL>() +
             check_cfg<T, OP, 9, COL>() + check_cfg<T, OP, 10, COL>();
-  if (!COL) bad += check_cfg<T, OP, 11, COL>() + check_cfg<T, OP, 12, COL>();
+  if (!COL) bad += check_cfg<T, OP, 11, COL>() + check_cfg<T, OP, 12, COL>() + check_cfg<T, OP, 13, COL>();
   return bad;
 }
 

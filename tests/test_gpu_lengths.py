@@ -176,3 +176,41 @@ def test_host_r2c_c2r_pipelined(rg, cuda, shape, axes, pinned):
     want_y = np.empty(shape, np.float64)
     P.c2r(X.astype(np.complex128), want_y, list(axes), False, 1.0 / n, 8)
     assert oracle.rel_l2(y, want_y) <= TOL[np.dtype(np.float32)]
+
+
+# The upper end of the 2^10 .. 2^24 range (the on-chip kernels stop at 8192 complex points):
+# four-step lengths with 2048- and 4096-point sides, a non-power-of-two split (3 * 2^21), and
+# real transforms whose half length is past one CTA.
+RANGE_TOP = [(2**21, 2), (2**22, 2), (2**23, 1), (2**24, 1), (3 * 2**21, 1)]
+
+
+@pytest.mark.parametrize("n,rows", RANGE_TOP)
+def test_c2c_r2c_range_top(rg, cuda, n, rows):
+    """complex64 c2c and float32 r2c / c2r at 2^21 .. 2^24 and 3 * 2^21 against the oracle's
+    double-precision result (relative L2 <= 1e-6), plus the inverse of each forward result
+    (round trip to the input within 2e-6)."""
+    torch = cuda
+    rng = np.random.default_rng(45)
+    P = oracle.port()
+    ax = np.array([1], np.int64)
+    x = (rng.standard_normal((rows, n)) + 1j * rng.standard_normal((rows, n))).astype(np.complex64)
+    want = np.empty((rows, n), np.complex128)
+    P.c2c(x.astype(np.complex128), want, [1], True, 1.0, 8)
+    xd = torch.from_numpy(x).cuda()
+    X = torch.empty_like(xd)
+    rg.c2c(xd, X, ax, True, 1.0, 1)
+    assert oracle.rel_l2(X.cpu().numpy(), want) <= 1e-6, n
+    back = torch.empty_like(xd)
+    rg.c2c(X, back, ax, False, 1.0 / n, 1)
+    assert oracle.rel_l2(back.cpu().numpy(), x) <= 2e-6, n
+    del xd, X, back
+    r = rng.standard_normal((rows, n)).astype(np.float32)
+    want_r = np.empty((rows, n // 2 + 1), np.complex128)
+    P.r2c(r.astype(np.float64), want_r, [1], True, 1.0, 8)
+    rd = torch.from_numpy(r).cuda()
+    R = torch.empty((rows, n // 2 + 1), dtype=torch.complex64, device="cuda")
+    rg.r2c(rd, R, ax, True, 1.0, 1)
+    assert oracle.rel_l2(R.cpu().numpy(), want_r) <= 1e-6, n
+    rb = torch.empty_like(rd)
+    rg.c2r(R, rb, ax, False, 1.0 / n, 1)
+    assert oracle.rel_l2(rb.cpu().numpy(), r) <= 2e-6, n
