@@ -242,6 +242,41 @@ def base_line(metric, value, unit, world, args, ms, dtype, config):
             "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)", "config": config}
 
 
+C1_FLOPS = 5 * 4096 * 12 * 256  # 5 n log2 n per transform, 256 transforms per step
+
+
+def fp64_roofline(rg, ms_per_step):
+    """The complex128 step against the device's FP64 fused multiply-add throughput (measured
+    here: rocketgpu_fp64_peak), counting 5 n log2 n flops per transform."""
+    peak = rg.fp64_peak() / 1e3  # TFLOP/s
+    achieved = C1_FLOPS / (ms_per_step / 1e3) / 1e12
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "measured (rocketgpu_fp64_peak, independent FMA chains)",
+            "flops_per_step": C1_FLOPS, "flop_count": "5 n log2 n per transform"}
+
+
+def c1_form(torch, rg, steps):
+    """complex128 c2c 256 x 4096 on device arrays (16 rotating inputs > L2): transforms/s and the
+    FP64 roofline, for the default line's forms."""
+    shape, axes = (256, 4096), np.array([1], dtype=np.int64)
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    xs = [torch.complex(torch.randn(shape, device="cuda", dtype=torch.float64, generator=gen),
+                        torch.randn(shape, device="cuda", dtype=torch.float64, generator=gen)) for _ in range(16)]
+    ys = [torch.empty_like(x) for x in xs]
+    for i in range(3):
+        rg.c2c(xs[i], ys[i], axes, True, 1.0, 1)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for i in range(steps):
+        rg.c2c(xs[i % 16], ys[i % 16], axes, True, 1.0, 1)
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    return {"workload": "c2c complex128 256 x 4096, axes [1], forward", "value": 256 / (ms / 1e3),
+            "unit": "transforms/s", "ms_per_step": ms, "roofline_fp64": fp64_roofline(rg, ms)}
+
+
 def run_c1(args):
     """Config 1: c2c complex128, batch 256 x length 4096, axes [1], forward, fct 1."""
     import torch
@@ -286,12 +321,12 @@ def run_c1(args):
     for _ in range(args.steps):
         rg.c2c(nx, ny, axes, True, 1.0, 1)
     e2e_rate = 256 * args.steps / (time.perf_counter() - t0)
-    flops = 5 * 4096 * 12 * 256
     line = base_line(METRIC, value, "transforms/s", world, args, ms, "f64",
                      {"workload": "c2c complex128 256 x 4096, axes [1], forward, fct 1", "global_batch": 256 * world,
                       "l2": f"inputs rotate over {rot} arrays ({rot * 16.8:.0f} MB) > L2",
-                      "fp64_tflops": flops * args.steps / (ms / 1e3) / 1e12})
-    line.update({"roofline": roof, "kernels": kernels, "accuracy": acc,
+                      "fp64_tflops": C1_FLOPS * args.steps / (ms / 1e3) / 1e12})
+    line.update({"roofline": roof, "roofline_fp64": fp64_roofline(rg, ms / args.steps), "kernels": kernels,
+                 "accuracy": acc,
                  "cpu_baseline": {"value": cpu_rate, "unit": "transforms/s", "cores": cores, "kind": "port",
                                   "sample": f"5 calls of 256 x 4096, nthreads={cores}"},
                  "e2e": {"value": e2e_rate, "unit": "transforms/s", "h2d_bytes_per_step": int(nx.nbytes),
@@ -743,6 +778,9 @@ def run_ours(args):
                       "c2c_frac": round(r["c2c_frac"], 3), "r2c_ms": round(r["r2c_ms"], 4),
                       "r2c_frac": round(r["r2c_frac"], 3)} for r in rows]}
 
+    # complex128 (config 1) beside it: rate and FP64 roofline
+    c1 = c1_form(torch, rg, args.steps) if rank == 0 else None
+
     # e2e: the same round trip through the C ABI on pinned host arrays
     e2e = None
     if rank == 0:
@@ -797,7 +835,7 @@ def run_ours(args):
             "accuracy": acc,
             "forms": {"plain_fp32": {"value": value, "ms_per_step": ms / args.steps,
                                      "r2c_rel_l2_vs_fp64": acc.get("r2c_rel_l2_vs_fp64")},
-                      "tc_split_fp16": tc_form},
+                      "tc_split_fp16": tc_form, "complex128_c1": c1},
             "length_range": length_range,
             "cpu_baseline": cpu,
             "e2e": e2e,

@@ -258,6 +258,11 @@ int rocketgpu_tc_error(void *stream);
  * flag), 0 otherwise, a negative status on failure. Synchronises `stream`. */
 int rocketgpu_long_error(void *stream);
 
+/* Measurement aid (no reference counterpart): FP64 fused multiply-add throughput of the current
+ * device in GFLOP/s, from a kernel of independent FMA chains timed with CUDA events on `stream`
+ * (best of three launches) -- the FP64 roofline of the complex128 transforms. */
+int rocketgpu_fp64_peak(double *gflops, void *stream);
+
 /* Two-axis plane kernels (no reference counterpart; off unless switched on here or by
  * ROCKET_GPU_PLANE=1). While on, an r2c over two or more axes whose last axis (contiguous, even
  * power-of-two length) and the axis before it fit one of the compiled plane sizes runs those

@@ -20,6 +20,7 @@ the reference's low-level signatures, host arrays only):
 from __future__ import annotations
 
 import ctypes
+import os
 import subprocess
 from pathlib import Path
 
@@ -28,7 +29,6 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_SO = HERE / "libpocketfft_port.so"
 REF_SO = HERE / "_ref" / "libpocketfft_ref.so"
-REF_SRC = Path("/root/reference/rocket_fft")
 
 
 class _Struct(ctypes.Structure):
@@ -161,10 +161,13 @@ def build_port():
     subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
 
 
-def build_ref():
-    """Compile the reference header into oracle/_ref when the reference tree is present."""
-    if (REF_SRC / "_pocketfft_hdronly.h").exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
+def build_ref(ref_src=None):
+    """Compile the reference header into oracle/_ref. `ref_src` is the reference's
+    ``rocket_fft`` directory (else the ROCKET_FFT_REF_SRC environment variable); nothing is built
+    when neither names a directory holding ``_pocketfft_hdronly.h``."""
+    src = ref_src or os.environ.get("ROCKET_FFT_REF_SRC")
+    if src and (Path(src) / "_pocketfft_hdronly.h").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={src}"], check=True)
 
 
 _port = None

@@ -35,6 +35,7 @@ from .pocketfft import (  # noqa: F401
     set_plane_kernels,
     tc_error,
     long_error,
+    fp64_peak,
     tc_selftest,
     version,
 )

@@ -96,6 +96,8 @@ def _declare(lib):
     lib.rocketgpu_set_plane_kernels.restype = i32
     lib.rocketgpu_tc_error.argtypes = [P]
     lib.rocketgpu_tc_error.restype = i32
+    lib.rocketgpu_fp64_peak.argtypes = [P, P]
+    lib.rocketgpu_fp64_peak.restype = i32
     lib.rocketgpu_long_error.argtypes = [P]
     lib.rocketgpu_long_error.restype = i32
     lib.rocketgpu_tc_selftest.argtypes = [P, P, P, P, P, P]

@@ -835,6 +835,13 @@ RG_EXPORT int rocketgpu_tc_error(void *stream) {
   return st == RG_OK ? flag : -st;
 }
 
+RG_EXPORT int rocketgpu_fp64_peak(double *gflops, void *stream) {
+  return guarded([&] {
+    RG_CHECK(gflops != nullptr, RG_ERR_ARG, "gflops is NULL");
+    *gflops = rg::fp64_peak_gflops(static_cast<cudaStream_t>(stream));
+  });
+}
+
 RG_EXPORT int rocketgpu_long_error(void *stream) {
   int flag = 0;
   const int st = guarded([&] { flag = rg::long_error_flag(static_cast<cudaStream_t>(stream)); });

@@ -102,6 +102,9 @@ void long_c2r(int64_t n, const void *in, const Side &ld, void *out, const Side &
 // 1 if a long-transform kernel gave up waiting on another CTA since the last call (cleared).
 int long_error_flag(cudaStream_t st);
 
+// FP64 fused multiply-add throughput of the current device, GFLOP/s (rg_probe.cu).
+double fp64_peak_gflops(cudaStream_t st);
+
 uint64_t launch_count();
 void note_launch();
 

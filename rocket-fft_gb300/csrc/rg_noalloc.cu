@@ -17,15 +17,16 @@
 //    (rows * n * itemsize) must fit in kScratchBytes, otherwise the call returns
 //    RG_ERR_UNSUPPORTED with a message naming the limit and does nothing;
 //  * the array is shared by all calls and keeps the last call's contents; each call rewrites
-//    the part it reads before reading it (tables are uploaded, the workspace is fully written
-//    by the four-step first pass), so nothing needs to start at zero. Calls whose GPU work
+//    the part it reads before reading it (a kernel computes the tables into it from parameters
+//    passed by value, the workspace is fully written by the four-step first pass), so nothing
+//    needs to start at zero and no host memory is read by the GPU. Calls whose GPU work
 //    overlaps (different streams, or different host threads without ordering) race on it;
-//  * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
-//    for that device; make that first call before any stream capture.
+//  * the first call in a CUDA context of a device looks up the array's device address in that
+//    context (cudaGetSymbolAddress); make that first call before any stream capture. Arrays
+//    must live on the current device.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <complex>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -48,21 +49,47 @@ namespace {
 
 constexpr size_t kAlign = 256;
 
-// Device address of the scratch array for the current device (looked up once per device).
+// The driver's current context, through the runtime's driver entry point (no link against the
+// driver library); nullptr when the entry point is unavailable.
+void *current_context() {
+  using Fn = int (*)(void **);
+  static Fn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return Fn(nullptr);
+    }
+    return reinterpret_cast<Fn>(f);
+  }();
+  void *ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
+
+// Device address of the scratch array in the current device and context. A __device__ array
+// has one instance per context, so the address is looked up once per (device, context); when
+// the context cannot be identified it is looked up on every call (the lookup allocates nothing).
 void *scratch_address() {
+  struct Ent {
+    int dev;
+    void *ctx, *addr;
+  };
   static std::mutex mu;
-  static void *addr[64] = {};
+  static std::vector<Ent> cache;
   int dev = 0;
   RG_CUDA(cudaGetDevice(&dev));
-  RG_CHECK(dev >= 0 && dev < 64, RG_ERR_UNSUPPORTED, "device index out of range");
+  void *ctx = current_context();  // nullptr before the runtime has made a context current
   std::lock_guard<std::mutex> lk(mu);
-  if (!addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) rg::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
-    addr[dev] = p;
-  }
-  return addr[dev];
+  if (ctx)
+    for (const Ent &e : cache)
+      if (e.dev == dev && e.ctx == ctx) return e.addr;
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) rg::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+  if (ctx) cache.push_back({dev, ctx, p});
+  return p;
 }
 
 thread_local int t_status = RG_OK;
@@ -76,13 +103,18 @@ struct Arr {
   std::vector<int64_t> shape, stride;  // stride in elements
 };
 
-bool is_device(const void *p) {
+// 1: device (or managed) memory of the current device; 0: not device memory; -1: device
+// memory of another device.
+int device_memory(const void *p) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return 0;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) return 0;
+  int dev = 0;
+  RG_CUDA(cudaGetDevice(&dev));
+  return at.type == cudaMemoryTypeManaged || at.device == dev ? 1 : -1;
 }
 
 Arr parse(uint64_t ndim, const rocketgpu_arystruct_t *a, const char *name) {
@@ -101,34 +133,69 @@ Arr parse(uint64_t ndim, const rocketgpu_arystruct_t *a, const char *name) {
 
 // ---- on-device layout: [tables...][workspace], every block 256-byte aligned -------------
 
-struct Arena {
-  DType dt;
-  std::vector<unsigned char> host;  // table bytes, uploaded in one copy
-  size_t ws_bytes = 0;
-
-  size_t put(const std::vector<std::complex<double>> &v) {
-    size_t off = (host.size() + kAlign - 1) / kAlign * kAlign;
-    const size_t es = rg::cx_size(dt);
-    host.resize(off + std::max<size_t>(v.size(), 1) * es, 0);
-    for (size_t i = 0; i < v.size(); ++i) {
-      if (dt == DType::F64) {
-        const double d[2] = {v[i].real(), v[i].imag()};
-        std::memcpy(&host[off + i * 16], d, 16);
-      } else {
-        const float f[2] = {float(v[i].real()), float(v[i].imag())};
-        std::memcpy(&host[off + i * 8], f, 8);
-      }
-    }
-    return off;
-  }
-  size_t tables_bytes() const { return (host.size() + kAlign - 1) / kAlign * kAlign; }
+// One block of twiddles W_N^t = e^{-2 pi i t / N} in the scratch array: entry i has
+// t = (i mod ns) * (i / ns + 1) (the radix-pass layout: (k - 1) * Ns + m -> m k) when ns > 0,
+// else t = i * step (split tables).
+struct TwSeg {
+  uint64_t off;   // byte offset in the scratch array
+  uint64_t N, step;
+  uint32_t count, ns;
+};
+constexpr int kMaxSegs = 40;
+struct TwFill {
+  TwSeg seg[kMaxSegs];
+  int nseg, f64;
 };
 
-std::complex<double> wfwd(uint64_t t, uint64_t N) {
-  double c, s;
-  rg::unit_root(t, N, c, s);
-  return {c, -s};
+// Computes the tables on the device from the descriptors (kernel parameters, passed by value):
+// the angle 2 pi t / N as sincospi(2t / N) in double (2t and N exact in double), rounded once
+// to the transform precision. One CTA row per descriptor.
+__global__ void __launch_bounds__(256) noalloc_tables(unsigned char *base, const __grid_constant__ TwFill f) {
+  const TwSeg sg = f.seg[blockIdx.y];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sg.count; i += gridDim.x * blockDim.x) {
+    uint64_t t = sg.ns ? uint64_t(i % sg.ns) * uint64_t(i / sg.ns + 1) : uint64_t(i) * sg.step;
+    t %= sg.N;
+    double sn, cs;
+    sincospi(double(2 * t) / double(sg.N), &sn, &cs);
+    if (f.f64)
+      reinterpret_cast<double2 *>(base + sg.off)[i] = make_double2(cs, -sn);
+    else
+      reinterpret_cast<float2 *>(base + sg.off)[i] = make_float2(float(cs), float(-sn));
+  }
 }
+
+struct Arena {
+  DType dt;
+  size_t bytes = 0;  // tables so far
+  std::vector<TwSeg> segs;
+  size_t ws_bytes = 0;
+
+  // room for `count` entries; returns the block's byte offset
+  size_t put(uint64_t count, uint64_t N, uint32_t ns, uint64_t step) {
+    const size_t off = (bytes + kAlign - 1) / kAlign * kAlign;
+    bytes = off + std::max<size_t>(count, 1) * rg::cx_size(dt);
+    if (count > 0) segs.push_back({off, N, step, uint32_t(count), ns});
+    return off;
+  }
+  size_t tables_bytes() const { return (bytes + kAlign - 1) / kAlign * kAlign; }
+
+  void fill(unsigned char *base, cudaStream_t st) const {
+    for (size_t s0 = 0; s0 < segs.size(); s0 += kMaxSegs) {
+      TwFill f{};
+      f.nseg = int(std::min<size_t>(kMaxSegs, segs.size() - s0));
+      f.f64 = dt == DType::F64 ? 1 : 0;
+      uint32_t most = 1;
+      for (int k = 0; k < f.nseg; ++k) {
+        f.seg[k] = segs[s0 + size_t(k)];
+        most = std::max(most, f.seg[k].count);
+      }
+      const unsigned gx = std::min<unsigned>(64, (most + 255) / 256);
+      noalloc_tables<<<dim3(gx, unsigned(f.nseg)), 256, 0, st>>>(base, f);
+      rg::note_launch();
+      RG_CUDA(cudaGetLastError());
+    }
+  }
+};
 
 // Pass descriptors + twiddles of an on-chip FFT of length L (Stockham radix passes, the
 // same schedule the cached plans use); core.tw is filled in once the arena has an address.
@@ -141,24 +208,31 @@ CoreRef add_core(Arena &ar, int L) {
   CoreRef c{};
   const std::vector<int> rad = rg::core_radices(L);
   RG_CHECK(int(rad.size()) <= rg::kMaxPass, RG_ERR_UNSUPPORTED, "too many passes");
-  std::vector<std::complex<double>> tw;
   c.core.L = L;
   c.core.npass = int(rad.size());
-  int Ns = 1;
+  // the passes' twiddles back to back: pass p with Ns > 1 holds W_{Ns R}^{m k} at
+  // (k - 1) Ns + m, from entry pd.tw on
+  int Ns = 1, total = 0;
   for (int p = 0; p < c.core.npass; ++p) {
     rg::PassDesc &pd = c.core.pass[p];
     pd.R = rad[p];
     pd.Ns = Ns;
     pd.LR = L / pd.R;
-    pd.tw = int(tw.size());
+    pd.tw = total;
     pd.dNs = rg::make_fastdiv(uint32_t(Ns));
     pd.dLR = rg::make_fastdiv(uint32_t(pd.LR));
-    if (Ns > 1)
-      for (int k = 1; k < pd.R; ++k)
-        for (int m = 0; m < Ns; ++m) tw.push_back(wfwd(uint64_t(m) * k, uint64_t(Ns) * pd.R));
+    if (Ns > 1) total += (pd.R - 1) * Ns;
     Ns *= pd.R;
   }
-  c.off = ar.put(tw);
+  c.off = (ar.bytes + kAlign - 1) / kAlign * kAlign;  // the block's start (entries follow per pass)
+  for (int p = 0; p < c.core.npass; ++p) {
+    const rg::PassDesc &pd = c.core.pass[p];
+    if (pd.Ns == 1) continue;
+    const uint64_t cnt = uint64_t(pd.R - 1) * pd.Ns;
+    ar.segs.push_back({c.off + size_t(pd.tw) * rg::cx_size(ar.dt), uint64_t(pd.Ns) * pd.R, 0, uint32_t(cnt),
+                       uint32_t(pd.Ns)});
+  }
+  ar.bytes = c.off + std::max<size_t>(total, 1) * rg::cx_size(ar.dt);
   return c;
 }
 
@@ -172,12 +246,9 @@ SplitRef add_split(Arena &ar, uint64_t N) {
   while ((uint64_t(1) << bits) < N) ++bits;
   const int shift = (bits + 1) / 2;
   const uint64_t nlo = uint64_t(1) << shift, nhi = (N + nlo - 1) / nlo;
-  std::vector<std::complex<double>> lo(nlo), hi(nhi);
-  for (uint64_t t = 0; t < nlo; ++t) lo[t] = wfwd(t, N);
-  for (uint64_t t = 0; t < nhi; ++t) hi[t] = wfwd(t * nlo, N);
   SplitRef s{};
-  s.lo = ar.put(lo);
-  s.hi = ar.put(hi);
+  s.lo = ar.put(nlo, N, 0, 1);    // W_N^t, t < 2^shift
+  s.hi = ar.put(nhi, N, 0, nlo);  // W_N^{t 2^shift}
   s.shift = shift;
   return s;
 }
@@ -324,8 +395,11 @@ void run(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t 
   for (int64_t s : in.shape)
     if (s == 0) return;
   if (ax.empty()) return;
-  RG_CHECK(is_device(in.data) && is_device(out.data), RG_ERR_UNSUPPORTED,
+  const int din = device_memory(in.data), dout = device_memory(out.data);
+  RG_CHECK(din != 0 && dout != 0, RG_ERR_UNSUPPORTED,
            "rocketgpu_c2c_noalloc takes device arrays only (host arrays need staging buffers)");
+  RG_CHECK(din == 1 && dout == 1, RG_ERR_ARG,
+           "rocketgpu_c2c_noalloc: the arrays live on another device than the current one");
   RG_CHECK(reinterpret_cast<uintptr_t>(in.data) % uintptr_t(in.itemsize) == 0 &&
                reinterpret_cast<uintptr_t>(out.data) % uintptr_t(out.itemsize) == 0,
            RG_ERR_UNSUPPORTED, "device data must be aligned to its item size");
@@ -361,8 +435,7 @@ void run(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocketgpu_arystruct_t 
                std::to_string(kScratchBytes) + " bytes (32 MiB)");
 
   char *base = static_cast<char *>(scratch_address());
-  if (!ar.host.empty())
-    RG_CUDA(cudaMemcpyAsync(base, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice, st));
+  ar.fill(reinterpret_cast<unsigned char *>(base), st);
   void *ws = base + ar.tables_bytes();
 
   for (size_t k = 0; k < plans.size(); ++k) {

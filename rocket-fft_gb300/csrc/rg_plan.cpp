@@ -204,43 +204,6 @@ template <class Obj, class Build> std::shared_ptr<Obj> cached(const Key &k, Buil
   return obj;
 }
 
-// Forward FFT of length m on the host in double (used once per Bluestein plan).
-void host_fft(std::vector<std::complex<double>> &x) {
-  const uint64_t m = x.size();
-  if (m <= 1) return;
-  std::vector<std::complex<double>> w(m);
-  for (uint64_t t = 0; t < m; ++t) w[t] = wfwd(t, m);
-  std::vector<uint64_t> rad;
-  {
-    uint64_t r = m;
-    for (uint64_t p : {4, 2, 3, 5, 7, 11, 13})
-      while (r % p == 0) {
-        rad.push_back(p);
-        r /= p;
-      }
-    if (r != 1) throw Error(RG_ERR_INTERNAL, "host_fft: length not 13-smooth");
-  }
-  std::vector<std::complex<double>> y(m);
-  uint64_t Ns = 1;
-  std::vector<std::complex<double>> v(16), o(16);
-  for (uint64_t R : rad) {
-    const uint64_t LR = m / R;
-    for (uint64_t j = 0; j < LR; ++j) {
-      const uint64_t mm = j % Ns;
-      for (uint64_t k = 0; k < R; ++k) v[k] = x[j + k * LR] * w[(mm * k * (m / (Ns * R))) % m];
-      for (uint64_t q = 0; q < R; ++q) {
-        std::complex<double> acc = 0;
-        for (uint64_t k = 0; k < R; ++k) acc += v[k] * w[((q * k) % R) * (m / R)];
-        o[q] = acc;
-      }
-      const uint64_t base = (j - mm) * R + mm;
-      for (uint64_t k = 0; k < R; ++k) y[base + k * Ns] = o[k];
-    }
-    x.swap(y);
-    Ns *= R;
-  }
-}
-
 }  // namespace
 
 static std::shared_ptr<CoreTables> core_ptr(int L, DType dt) {
@@ -312,29 +275,48 @@ SplitTables get_split(uint64_t N, DType dt) {
 }
 
 const BlueTables &get_blue(uint64_t n, DType dt) {
-  Key k{current_device(), int(dt), 4, n, 0};
-  auto r = cached<BlueTables>(k, [&](BlueTables &o, Entry &e) {
-    const uint64_t m = blue_length(n);
-    std::vector<std::complex<double>> bk(n), b(m, 0.0);
-    for (uint64_t j = 0; j < n; ++j) {
-      const uint64_t t = uint64_t(((unsigned __int128)j * j) % (2 * n));
-      double c, s;
-      unit_root(t, 2 * n, c, s);
-      bk[j] = {c, s};
-    }
-    b[0] = bk[0];
-    for (uint64_t j = 1; j < n; ++j) b[j] = b[m - j] = bk[j];
-    host_fft(b);
-    const double inv = 1.0 / double(m);
-    for (auto &z : b) z *= inv;
-    o.n = n;
-    o.m = m;
-    o.bk = upload(bk, dt, e.bytes);
-    o.bkf = upload(b, dt, e.bytes);
-    e.dptrs.push_back(const_cast<void *>(o.bk));
-    e.dptrs.push_back(const_cast<void *>(o.bkf));
-  });
-  return *r;
+  const Key k{current_device(), int(dt), 4, n, 0};
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cache.find(k);
+    if (it != g_cache.end()) return *std::static_pointer_cast<BlueTables>(it->second.obj);
+  }
+  // built outside the cache lock: the device construction runs the library's own FFT, which
+  // takes plans from this cache
+  const uint64_t m = blue_length(n);
+  auto obj = std::make_shared<BlueTables>();
+  Entry e;
+  void *bk = nullptr, *bkf = nullptr;
+  RG_CUDA(cudaMalloc(&bk, std::max<uint64_t>(n, 1) * cx_size(dt)));
+  if (cudaMalloc(&bkf, std::max<uint64_t>(m, 1) * cx_size(dt)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(bk);
+    throw Error(RG_ERR_NOMEM, "cudaMalloc failed for Bluestein tables");
+  }
+  try {
+    blue_tables_device(n, m, dt, bk, bkf);
+  } catch (...) {
+    cudaFree(bk);
+    cudaFree(bkf);
+    throw;
+  }
+  obj->n = n;
+  obj->m = m;
+  obj->bk = bk;
+  obj->bkf = bkf;
+  e.dptrs = {bk, bkf};
+  e.bytes = size_t(n + m) * cx_size(dt);
+  e.obj = obj;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_cache.find(k);
+  if (it != g_cache.end()) {  // another thread built the same tables meanwhile
+    cudaFree(bk);
+    cudaFree(bkf);
+    return *std::static_pointer_cast<BlueTables>(it->second.obj);
+  }
+  g_bytes += e.bytes;
+  g_cache.emplace(k, std::move(e));
+  return *obj;
 }
 
 void cache_clear() {

@@ -54,6 +54,10 @@ struct BlueTables {
 };
 const BlueTables &get_blue(uint64_t n, DType dt);
 
+// Fill device tables bk (n entries) and bkf (m entries) in the precision dt (rg_plan_dev.cu);
+// synchronous.
+void blue_tables_device(uint64_t n, uint64_t m, DType dt, void *bk, void *bkf);
+
 // Smallest 13-smooth length usable as the Bluestein convolution length for n.
 uint64_t blue_length(uint64_t n);
 

@@ -97,6 +97,18 @@ def _empty(like, shape, dtype):
     return np.empty(tuple(shape), dtype=dtype)
 
 
+def _dest(like, shape, dtype, out):
+    """The output array: `out` itself when given (it must have the result's shape and dtype and
+    live where the input does: both NumPy arrays or both tensors on one device), else a new
+    array like `like`."""
+    if out is None:
+        return _empty(like, shape, dtype)
+    if tuple(out.shape) != tuple(shape) or out.dtype != dtype or _is_torch(out) != _is_torch(like) or (
+            _is_torch(out) and out.device != like.device):
+        raise ValueError("out must have the shape and dtype of the result")
+    return out
+
+
 def _zeros(like, shape, dtype):
     if _is_torch(like):
         return _torch.zeros(tuple(shape), dtype=dtype, device=like.device)
@@ -253,7 +265,7 @@ def _axes_arg(axes):
 # generic transforms (rocket_fft/overloads.py:943-1045)
 # ---------------------------------------------------------------------------------------------
 
-def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=None):
+def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=None, dest=None):
     x = _asarray(x)
     s, axes = _shape_and_axes(x, s, axes, unique)
     shape = list(x.shape)
@@ -263,18 +275,21 @@ def _c2cn(x, s, axes, norm, overwrite_x, forward, unique=None):
     cdt = _dtype(x, True)
     if _kind(x) == "c":
         xin = _resize(_cast(x, cdt), shape)
-        out = xin if (overwrite_x or xin is not x) else _empty(xin, shape, cdt)
+        if dest is not None:
+            out = _dest(xin, shape, cdt, dest)
+        else:
+            out = xin if (overwrite_x or xin is not x) else _empty(xin, shape, cdt)
         fct = _fct(shape, axes, norm, forward)
         _pf.c2c(xin, out, _axes_arg(axes), forward, fct, 1)
         return out
     xin = _resize(_cast(x, _dtype(x, False)), shape)
-    out = _empty(xin, shape, cdt)
+    out = _dest(xin, shape, cdt, dest)
     fct = _fct(shape, axes, norm, forward)
     _pf.c2c_sym(xin, out, _axes_arg(axes), forward, fct, 1)
     return out
 
 
-def _r2cn(x, s, axes, norm, forward, unique=None):
+def _r2cn(x, s, axes, norm, forward, unique=None, dest=None):
     x = _asarray(x)
     if _kind(x) == "c":
         raise TypeError("x must be a real sequence")
@@ -286,13 +301,13 @@ def _r2cn(x, s, axes, norm, forward, unique=None):
     xin = _resize(_cast(x, _dtype(x, False)), shape)
     oshape = list(shape)
     oshape[axes[-1]] = shape[axes[-1]] // 2 + 1
-    out = _empty(xin, oshape, _dtype(x, True))
+    out = _dest(xin, oshape, _dtype(x, True), dest)
     fct = _fct(shape, axes, norm, forward)
     _pf.r2c(xin, out, _axes_arg(axes), forward, fct, 1)
     return out
 
 
-def _c2rn(x, s, axes, norm, forward, unique=None):
+def _c2rn(x, s, axes, norm, forward, unique=None, dest=None):
     x = _asarray(x)
     s, axes = _shape_and_axes(x, s, axes, unique)
     last = axes[-1]
@@ -306,7 +321,7 @@ def _c2rn(x, s, axes, norm, forward, unique=None):
     ishape = list(oshape)
     ishape[last] = oshape[last] // 2 + 1
     xin = _resize(_cast(x, _dtype(x, True)), ishape)
-    out = _empty(xin, oshape, _dtype(x, False))
+    out = _dest(xin, oshape, _dtype(x, False), dest)
     fct = _fct(oshape, axes, norm, forward)
     _pf.c2r(xin, out, _axes_arg(axes), forward, fct, 1)
     return out

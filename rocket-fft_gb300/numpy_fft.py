@@ -22,75 +22,66 @@ __all__ = [
 ]
 
 
-def _out(res, out):
-    if out is None:
-        return res
-    if tuple(out.shape) != tuple(res.shape) or out.dtype != res.dtype:
-        raise ValueError("out must have the shape and dtype of the result")
-    out[...] = res
-    return out
-
-
 def fft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2cn(a, s, axes, norm, False, True), out)
+    return _f._c2cn(a, s, axes, norm, False, True, dest=out)
 
 
 def ifft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2cn(a, s, axes, norm, False, False), out)
+    return _f._c2cn(a, s, axes, norm, False, False, dest=out)
 
 
 def fft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, True), out)
+    return _f._c2cn(a, s, axes, norm, False, True, dest=out)
 
 
 def ifft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, False), out)
+    return _f._c2cn(a, s, axes, norm, False, False, dest=out)
 
 
 def fftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, True), out)
+    return _f._c2cn(a, s, axes, norm, False, True, dest=out)
 
 
 def ifftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._c2cn(a, s, axes, norm, False, False), out)
+    return _f._c2cn(a, s, axes, norm, False, False, dest=out)
 
 
 def rfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._r2cn(a, s, axes, norm, True), out)
+    return _f._r2cn(a, s, axes, norm, True, dest=out)
 
 
 def irfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2rn(a, s, axes, norm, False), out)
+    return _f._c2rn(a, s, axes, norm, False, dest=out)
 
 
 def rfft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._r2cn(a, s, axes, norm, True), out)
+    return _f._r2cn(a, s, axes, norm, True, dest=out)
 
 
 def irfft2(a, s=None, axes=(-2, -1), norm=None, out=None):
-    return _out(_f._c2rn(a, s, axes, norm, False), out)
+    return _f._c2rn(a, s, axes, norm, False, dest=out)
 
 
 def rfftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._r2cn(a, s, axes, norm, True), out)
+    return _f._r2cn(a, s, axes, norm, True, dest=out)
 
 
 def irfftn(a, s=None, axes=None, norm=None, out=None):
-    return _out(_f._c2rn(a, s, axes, norm, False), out)
+    return _f._c2rn(a, s, axes, norm, False, dest=out)
 
 
 def hfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._c2rn(a, s, axes, norm, True), out)
+    return _f._c2rn(a, s, axes, norm, True, dest=out)
 
 
 def ihfft(a, n=None, axis=-1, norm=None, out=None):
     s, axes = _f._one_axis(n, axis)
-    return _out(_f._r2cn(a, s, axes, norm, False), out)
+    return _f._r2cn(a, s, axes, norm, False, dest=out)
 
 
 fftfreq = _f.fftfreq

@@ -429,6 +429,16 @@ def set_plane_kernels(on=True):
     return bool(_lib.load().rocketgpu_set_plane_kernels(1 if on else 0))
 
 
+def fp64_peak(stream=None):
+    """FP64 fused multiply-add throughput of the current device, GFLOP/s (a measurement aid:
+    the denominator of the complex128 roofline)."""
+    v = ctypes.c_double(0.0)
+    st = int(_lib.load().rocketgpu_fp64_peak(ctypes.byref(v), ctypes.c_void_p(_stream_int(stream)) if stream else None))
+    if st != 0:
+        _raise_status(st, "rocketgpu_fp64_peak")
+    return v.value
+
+
 def long_error(stream=None):
     """1 if a long-transform kernel gave up waiting on another of its tiles since the previous
     call (the flag is cleared), else 0."""

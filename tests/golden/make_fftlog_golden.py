@@ -7,21 +7,21 @@ r = logspace(-4, 4, 16), mu = 0.3: offset 0 and bias 0, then the optimal offset 
 through ``ast``; nothing of it is executed) and writes them to ``fftlog_fortran.json`` beside it.
 The reference tree is only needed to regenerate the file.
 
-Usage: python tests/golden/make_fftlog_golden.py
+Usage: python tests/golden/make_fftlog_golden.py <the reference's tests/test_fftlog.py>
 """
 
 from __future__ import annotations
 
 import ast
 import json
+import sys
 from pathlib import Path
 
-SRC = Path("/root/reference/tests/test_fftlog.py")
 OUT = Path(__file__).resolve().parent / "fftlog_fortran.json"
 
 
-def main():
-    tree = ast.parse(SRC.read_text())
+def main(src: Path):
+    tree = ast.parse(src.read_text())
     fn = next(n for n in ast.walk(tree) if isinstance(n, ast.FunctionDef) and n.name == "test_fht_agrees_with_fftlog")
     vectors = []
     for node in fn.body:  # top-level statements, in source order
@@ -42,4 +42,6 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fftlog_golden.py <the reference's tests/test_fftlog.py>")
+    main(Path(sys.argv[1]))

@@ -108,8 +108,10 @@ def run_case(c, rng, R):
 
 
 def main():
+    # the reference's rocket_fft directory comes from ROCKET_FFT_REF_SRC (or an already built
+    # oracle/_ref is used as it is)
     oracle.build_ref()
-    assert oracle.ref_available(), "the reference oracle could not be built"
+    assert oracle.ref_available(), "the reference oracle could not be built: set ROCKET_FFT_REF_SRC"
     R = oracle.ref()
     rng = np.random.default_rng(20261203)
     arrays = {}

@@ -8,6 +8,12 @@
 #include "rg_fixed_kernel.cuh"
 #include "rg_plan.hpp"
 
+// The planner's Bluestein tables are built by the library's kernels (rg_plan_dev.cu), which this
+// host-only check does not link; it builds no Bluestein plan.
+namespace rg {
+void blue_tables_device(uint64_t, uint64_t, DType, void *, void *) {}
+}  // namespace rg
+
 template <typename T, int OP, int E, bool COL> int check_cfg() {
   using C = rg::FxCfg<T, OP, E, COL>;
   if (C::SMEM > 227 * 1024) {

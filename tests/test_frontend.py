@@ -37,6 +37,13 @@ def test_norm_and_axes_validation(F, rg):
         F.rfft(x.astype(np.complex128))
     with pytest.raises(ValueError, match="negative"):
         F.next_fast_len(-1)
+    N = rg.numpy_fft  # numpy's out=: the result's shape and dtype, checked before any work
+    with pytest.raises(ValueError, match="out must"):
+        N.fft(x, out=np.empty((4, 5), np.complex128))
+    with pytest.raises(ValueError, match="out must"):
+        N.rfft(x, out=np.empty((4, 4), np.complex64))
+    with pytest.raises(ValueError, match="out must"):
+        N.irfft(x.astype(np.complex128), out=np.empty((4, 10), np.float32))
 
 
 def test_next_fast_len_matches_scipy(F):

@@ -159,6 +159,21 @@ def test_numpy_namespace(rg, cuda):
     res = rg.numpy_fft.ifft2(xd, out=out)
     assert res is out
     _cmp(out, np.fft.ifft2(x), np.complex128)
+    # out= is written by the transform itself: real input (c2c_sym), r2c, c2r, and out = input
+    r0 = _rand((6, 10), np.float64, 11)
+    rd = torch.from_numpy(r0).cuda()
+    o1 = torch.empty((6, 10), dtype=torch.complex128, device="cuda")
+    assert rg.numpy_fft.fft(rd, out=o1) is o1
+    _cmp(o1, np.fft.fft(r0), np.complex128)
+    o2 = torch.empty((6, 6), dtype=torch.complex128, device="cuda")
+    assert rg.numpy_fft.rfft(rd, out=o2) is o2
+    _cmp(o2, np.fft.rfft(r0), np.complex128)
+    o3 = torch.empty((6, 10), dtype=torch.float64, device="cuda")
+    assert rg.numpy_fft.irfft(o2, n=10, out=o3) is o3
+    _cmp(o3, r0, np.float64)
+    xi = xd.clone()
+    assert rg.numpy_fft.fft(xi, out=xi) is xi
+    _cmp(xi, np.fft.fft(x), np.complex128)
     r = _rand((5, 18), np.float64, 8)
     _cmp(rg.numpy_fft.rfft(torch.from_numpy(r).cuda(), n=20), np.fft.rfft(r, n=20), np.float64)
     _cmp(rg.numpy_fft.hfft(torch.from_numpy(x).cuda()), np.fft.hfft(x), np.float64)

@@ -87,3 +87,71 @@ def test_noalloc_rejects_host_arrays():
     x = np.zeros((4, 64), np.complex64)
     st, msg = _noalloc(rg, f, x, x.copy(), [1], True, 1.0, 0)
     assert st == 2 and "device arrays" in msg, (st, msg)
+
+
+def test_noalloc_against_oracle_and_in_place(cuda):
+    """Against the oracle's double result: complex128 through the two-pass workspace
+    (8 x 65536, 1e-13) and complex64 on chip in place (64 x 4096, 1e-6)."""
+    import oracle
+
+    torch = cuda
+    rg, f = _bind()
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((8, 65536)) + 1j * rng.standard_normal((8, 65536))
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    st, msg = _noalloc(rg, f, xd, yd, [1], True, 1.0, stream)
+    assert st == 0, msg
+    want = np.empty_like(x)
+    oracle.port().c2c(x, want, [1], True, 1.0, 8)
+    assert oracle.rel_l2(yd.cpu().numpy(), want) <= TOL[np.dtype(np.complex128)]
+    z = (rng.standard_normal((64, 4096)) + 1j * rng.standard_normal((64, 4096))).astype(np.complex64)
+    zd = torch.from_numpy(z).cuda()
+    st, msg = _noalloc(rg, f, zd, zd, [1], False, 1.0 / 4096, stream)
+    assert st == 0, msg
+    wz = np.empty(z.shape, np.complex128)
+    oracle.port().c2c(z.astype(np.complex128), wz, [1], False, 1.0 / 4096, 8)
+    assert oracle.rel_l2(zd.cpu().numpy(), wz) <= TOL[np.dtype(np.complex64)]
+
+
+def test_noalloc_scratch_boundary(cuda):
+    """complex64 rows of 65536 = 256 x 256 points need rows x 512 KiB of workspace plus about
+    8 KiB of tables: 63 rows fit in the 32 MiB array (and match the regular entry point), 64
+    rows do not and are rejected without work."""
+    torch = cuda
+    rg, f = _bind()
+    stream = torch.cuda.current_stream().cuda_stream
+    gen = torch.Generator(device="cuda").manual_seed(12)
+    x = torch.randn((63, 65536), dtype=torch.complex64, device="cuda", generator=gen)
+    got = torch.empty_like(x)
+    st, msg = _noalloc(rg, f, x, got, [1], True, 1.0, stream)
+    assert st == 0, msg
+    ref = torch.empty_like(x)
+    rg.c2c(x, ref, np.array([1]), True, 1.0, 1)
+    r, g = ref.cpu().numpy(), got.cpu().numpy()
+    assert np.linalg.norm(g - r) / np.linalg.norm(r) <= TOL[np.dtype(np.complex64)]
+    x64 = torch.zeros((64, 65536), dtype=torch.complex64, device="cuda")
+    y64 = torch.full_like(x64, 3.0)
+    st, msg = _noalloc(rg, f, x64, y64, [1], True, 1.0, stream)
+    assert st == 2 and "32 MiB" in msg, (st, msg)
+    assert bool((y64 == 3.0).all())
+
+
+def test_noalloc_sequence_of_dtypes_and_lengths(cuda):
+    """complex128 two-pass, complex64 on chip, complex128 two-pass again on one stream: each call
+    rewrites the tables and workspace it reads, so each matches the regular entry point."""
+    torch = cuda
+    rg, f = _bind()
+    stream = torch.cuda.current_stream().cuda_stream
+    gen = torch.Generator(device="cuda").manual_seed(13)
+    for dtype, shape in [("complex128", (4, 1 << 17)), ("complex64", (32, 2048)), ("complex128", (6, 3 * 4096))]:
+        tdt = getattr(torch, dtype)
+        x = torch.randn(shape, dtype=tdt, device="cuda", generator=gen)
+        got = torch.empty_like(x)
+        st, msg = _noalloc(rg, f, x, got, [1], True, 1.0, stream)
+        assert st == 0, msg
+        ref = torch.empty_like(x)
+        rg.c2c(x, ref, np.array([1]), True, 1.0, 1)
+        r, g = ref.cpu().numpy(), got.cpu().numpy()
+        assert np.linalg.norm(g - r) / np.linalg.norm(r) <= TOL[np.dtype(dtype)], dtype
