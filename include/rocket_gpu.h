@@ -245,7 +245,7 @@ int rocketgpu_c2c_noalloc(uint64_t ndim, const rocketgpu_arystruct_t *ain, rocke
  * plain FP32 kernels. rocketgpu_set_tc_split returns the previous setting.
  * rocketgpu_tc_error returns 1 if a tensor-core kernel gave up waiting for its matrix products
  * since the library was loaded (0 otherwise, negative status on failure).
- * rocketgpu_tc_selftest computes D = A B^T + A B2^T + A2 B^T + A2 B2^T on the tensor cores through the
+ * rocketgpu_tc_selftest computes D = A B^T + A B2^T + A2 B^T on the tensor cores through the
  * same operand layout, descriptors and tensor-memory path as the transform kernels: A, A2
  * 256 x 32, B, B2 32 x 32 float16 (row-major, device), D 256 x 32 float32 (device). */
 int rocketgpu_set_tc_split(int on);

@@ -8,7 +8,7 @@
 #include "rg_error.hpp"
 #include "rg_exec.hpp"
 #include "rg_launch.hpp"
-#include "rg_long.cuh"
+#include "rg_long_launch.cuh"
 #include "rg_plan.hpp"
 
 namespace rg {
@@ -35,68 +35,33 @@ int *error_word() {
   return words[dev & 63];
 }
 
-template <int KIND, int E1, int E2, int ET>
-void launch_long(LongArgs &a, int64_t tickets, cudaStream_t st) {
-  using Cf = LgCfg<E1, E2, ET>;
-  const void *fn = reinterpret_cast<const void *>(&long_kernel<KIND, E1, E2, ET>);
-  set_smem_attr(fn, Cf::SMEM);
-  const int64_t res = resident_ctas(fn, Cf::NT, Cf::SMEM);
-  RG_CHECK(res > 0, RG_ERR_INTERNAL, "long transform kernel does not fit on an SM");
-  const unsigned grid = unsigned(std::min<int64_t>(tickets, res));
-  long_kernel<KIND, E1, E2, ET><<<grid, Cf::NT, Cf::SMEM, st>>>(a);
-  note_launch();
-  RG_CUDA(cudaGetLastError());
-}
-
 struct Shape {
   int e1, e2, et;
 };
 
 // Split and tile per log2 length. n1 <= n2, so that phase A (which reads the input from HBM)
 // gets the wider segments; tiles of 2^13 elements (64 KB of shared memory) up to 2^22 points,
-// 2^14 (128 KB) above, where 2^13 would leave two-element segments.
+// 2^14 (128 KB) above, where 2^13 would leave two-element segments. ROCKET_GPU_LONG_ET_SHIFT
+// (-2 .. 0) takes smaller tiles (more CTAs per SM) where such an instance exists.
 Shape shape_for(int e) {
-  const int et_env = env_int("ROCKET_GPU_LONG_ET", 0);
+  Shape s{0, 0, 0};
   switch (e) {
-    case 14: return {7, 7, 11};
-    case 15: return {7, 8, 11};
-    case 16: return {8, 8, 12};
-    case 17: return {8, 9, 12};
-    case 18: return {9, 9, 13};
-    case 19: return {9, 10, 13};
-    case 20: return {10, 10, 13};
-    case 21: return {10, 11, 13};
-    case 22: return {11, 11, et_env == 14 ? 14 : 13};
-    case 23: return {11, 12, et_env == 13 ? 13 : 14};
-    case 24: return {12, 12, et_env == 13 ? 13 : 14};
-    default: return {0, 0, 0};
+    case 14: s = {7, 7, 11}; break;
+    case 15: s = {7, 8, 11}; break;
+    case 16: s = {8, 8, 12}; break;
+    case 17: s = {8, 9, 12}; break;
+    case 18: s = {9, 9, 13}; break;
+    case 19: s = {9, 10, 13}; break;
+    case 20: s = {10, 10, 13}; break;
+    case 21: s = {10, 11, 13}; break;
+    case 22: s = {11, 11, 13}; break;
+    case 23: s = {11, 12, 14}; break;
+    case 24: s = {12, 12, 14}; break;
+    default: return s;
   }
-}
-
-template <int KIND> bool dispatch(const Shape &s, LongArgs &a, int64_t tickets, cudaStream_t st) {
-#define RG_LONG_CASE(A, B, T)                   \
-  if (s.e1 == A && s.e2 == B && s.et == T) {    \
-    launch_long<KIND, A, B, T>(a, tickets, st); \
-    return true;                                \
-  }
-  RG_LONG_CASE(7, 7, 11)
-  RG_LONG_CASE(7, 8, 11)
-  RG_LONG_CASE(8, 8, 12)
-  RG_LONG_CASE(8, 9, 12)
-  RG_LONG_CASE(9, 9, 13)
-  RG_LONG_CASE(9, 10, 13)
-  RG_LONG_CASE(10, 10, 13)
-  RG_LONG_CASE(10, 11, 13)
-  RG_LONG_CASE(11, 11, 13)
-  RG_LONG_CASE(11, 11, 14)
-  RG_LONG_CASE(11, 12, 13)
-  RG_LONG_CASE(11, 12, 14)
-  if constexpr (KIND == LG_C2C) {  // real transforms stop at half length 2^23
-    RG_LONG_CASE(12, 12, 13)
-    RG_LONG_CASE(12, 12, 14)
-  }
-#undef RG_LONG_CASE
-  return false;
+  const int shift = env_int("ROCKET_GPU_LONG_ET_SHIFT", 0);
+  if (shift < 0 && shift >= -2 && long_shape_instantiated(s.e1, s.e2, s.et + shift)) s.et += shift;
+  return s;
 }
 
 bool strides_multiple(const Side &s, int64_t q) {
@@ -125,17 +90,22 @@ void run_long(int64_t m, const void *in, const Side &ld, void *out, const Side &
   RG_CHECK(s.e1 + s.e2 == log2_of(m), RG_ERR_INTERNAL, "no long-transform shape for this length");
   const int64_t tt = int64_t(1) << s.et;
   const int64_t ybytes = m * int64_t(cx_size(dt));
-  // group: about ROCKET_GPU_LONG_GROUP_MB (16) MiB of Y; ring of 3 buffers when three fit in
-  // 48 MiB, 2 when two fit in 64 MiB, else 1
-  const int64_t want = int64_t(env_int("ROCKET_GPU_LONG_GROUP_MB", 16)) << 20;
+  // group: about ROCKET_GPU_LONG_GROUP_MB (32) MiB of Y; ring: as many groups as fit in
+  // ROCKET_GPU_LONG_YMB (96) MiB, at most 8 (ROCKET_GPU_LONG_NBUF overrides); phase A runs
+  // S - 2 groups ahead of phase B (ROCKET_GPU_LONG_LOOK overrides, at most S - 1). Measured on
+  // GB300 (2^14 .. 2^22 points): 32 / 96 MiB ran 15-25 % faster than 8 / 64 MiB.
+  const int64_t want = int64_t(env_int("ROCKET_GPU_LONG_GROUP_MB", 32)) << 20;
+  const int64_t budget = int64_t(env_int("ROCKET_GPU_LONG_YMB", 96)) << 20;
   const int64_t G = std::max<int64_t>(1, std::min<int64_t>(nrows, want / ybytes));
   const int64_t ng = (nrows + G - 1) / G;
-  int nbuf = 1;
-  if (3 * G * ybytes <= (int64_t(48) << 20)) nbuf = 3;
-  else if (2 * G * ybytes <= (int64_t(64) << 20)) nbuf = 2;
+  int64_t nbuf = std::max<int64_t>(1, std::min<int64_t>(8, budget / (G * ybytes)));
   const int nenv = env_int("ROCKET_GPU_LONG_NBUF", 0);
-  if (nenv >= 1 && nenv <= 3) nbuf = nenv;
-  nbuf = int(std::min<int64_t>(nbuf, ng));
+  if (nenv >= 1 && nenv <= 16) nbuf = nenv;
+  nbuf = std::min<int64_t>(nbuf, ng);
+  int64_t look = std::max<int64_t>(0, nbuf - 2);
+  const int lenv = env_int("ROCKET_GPU_LONG_LOOK", -1);
+  if (lenv >= 0) look = lenv;
+  look = std::min<int64_t>({look, nbuf - 1, ng});
   const int64_t tiles = G * m / tt;
   const int64_t tickets = 2 * ng * tiles;
   RG_CHECK(tickets < (int64_t(1) << 31) && ng < (int64_t(1) << 28), RG_ERR_UNSUPPORTED,
@@ -155,8 +125,8 @@ void run_long(int64_t m, const void *in, const Side &ld, void *out, const Side &
   a.errw = error_word();
   a.G = int(G);
   a.ngroups = int(ng);
-  a.nbuf = nbuf;
-  a.look = nbuf >= 2 ? 1 : 0;
+  a.nbuf = int(nbuf);
+  a.look = int(look);
   a.tiles = int(tiles);
   a.conj_in = cin ? 1 : 0;
   a.conj_out = cout ? 1 : 0;
@@ -174,9 +144,10 @@ void run_long(int64_t m, const void *in, const Side &ld, void *out, const Side &
     a.shift2 = sp2.shift;
   }
   a.flags = (env_int("ROCKET_GPU_LONG_DISCARD", 1) ? kLongDiscard : 0) |
-            (env_int("ROCKET_GPU_LONG_EVICT_OUT", 0) ? kLongEvictOut : 0);
+            (env_int("ROCKET_GPU_LONG_EVICT_OUT", 1) ? kLongEvictOut : 0);
   profiled_launch(name, bytes, st, [&] {
-    RG_CHECK(dispatch<KIND>(s, a, tickets, st), RG_ERR_INTERNAL, "long-transform kernel not instantiated");
+    RG_CHECK(long_dispatch<KIND>(s.e1, s.e2, s.et, a, tickets, st), RG_ERR_INTERNAL,
+             "long-transform kernel not instantiated");
   });
 }
 

@@ -11,20 +11,24 @@
 //   phase B  for each row k1 of Y, an FFT of length n2 over j2, into X[k1 + n1 k2]
 //
 // A phase-A tile is C = TT / n1 adjacent columns of one transform (its HBM reads are C-element
-// segments, two columns per 16-byte load); a phase-B tile is D = TT / n2 adjacent rows of Y
-// (its HBM writes are D-element segments, two rows per 16-byte store). Both phases read their
-// first radix pass straight from global memory into registers and write their last pass straight
-// back; the passes in between run in place in one shared buffer.
+// segments: lanes run across the columns first); a phase-B tile is D = TT / n2 adjacent rows of
+// Y (its HBM writes are D-element segments). Each thread runs one radix butterfly per pass (at
+// most 64 registers, two CTAs of TT / 16 threads per SM). Both phases read their first radix
+// pass straight from global memory into registers and write their last pass straight back; the
+// passes in between run in place in one shared buffer, whose line pitch is chosen at compile
+// time to minimise shared-memory wavefronts over all of the kernel's access patterns.
 //
 // Y is the only intermediate, and it is kept in L2: transforms go through in groups of G
-// (G * n * 8 bytes of Y per group), and each group has its own region of a ring of nbuf Y
-// buffers. Every tile is a ticket taken from an atomic counter, in the order
-//     look = 1:  A0 A1 B0 A2 B1 ... A(g) B(g-1) ... B(last)      (nbuf >= 2)
-//     look = 0:  A0 B0 A1 B1 ...                                  (nbuf == 1)
+// (G * n * 8 bytes of Y per group), and group g uses slot g mod S of a ring of S Y buffers.
+// Every tile is a ticket taken from an atomic counter; phase A runs `look` groups ahead of
+// phase B, the tickets in the order
+//     A0 .. A(look-1), then A(g) B(g-look) for g = look .. ng-1, then the remaining B
 // A B(g) tile first waits until every A(g) tile is done; an A(g) tile waits until every
-// B(g - nbuf) tile has released its Y buffer. A CTA only ever waits on tickets below its own,
-// which running CTAs hold, so the launch always makes progress. Every wait is bounded (2 s of
-// %globaltimer): past it the CTA sets the error word and every CTA leaves its loop.
+// B(g - S) tile has released its slot (S >= look + 1). A CTA waits only on tickets below its
+// own; the lowest unfinished ticket is held by a running CTA and waits on nothing unfinished,
+// so the launch always makes progress (a CTA holds its next ticket while it works on the
+// current one, which keeps that true). Every wait is bounded (2 s of %globaltimer): past it the
+// CTA sets the error word and every CTA leaves its loop.
 // Y is written and read through L2 only (st/ld .cg), and a phase-B tile discards the Y lines it
 // has consumed (discard.global.L2), so dead intermediate data is never written back to HBM.
 //
@@ -51,7 +55,7 @@ struct LongArgs {
   void *ybuf;         // nbuf * G * n complex elements
   int *ctr;           // [0] ticket, [1] error, [2] unused, [3, 3+ng) A done, [3+ng, 3+2ng) B done
   int *errw;          // per-device error word: set when a wait gave up
-  int G, ngroups, nbuf, look;
+  int G, ngroups, nbuf, look;  // nbuf: ring slots S
   int tiles;          // tiles per phase and group (G * n / TT)
   int conj_in, conj_out;
   float fct;
@@ -72,19 +76,6 @@ namespace lg {
 
 // shared index of position pos of a line: one pad slot per 32 positions
 __host__ __device__ constexpr int sp(int pos) { return pos + (pos >> 5); }
-
-// Line pitch in shared slots for lines of length L accessed in the first / last pass by lanes
-// that run across `pairs` pairs of adjacent lines first (two lines per lane): lane (pair q, j)
-// lands on slot 2 q pitch + (a function of j taking 16 / pairs consecutive values), so the
-// pitch must be 8 / pairs modulo 8 for the 32 lanes to fill each of the 16 eight-byte slots of
-// a wavefront exactly twice.
-__host__ __device__ constexpr int pitch(int L, int pairs) {
-  int p = sp(L - 1) + 1;
-  const int want = pairs >= 2 && pairs <= 8 ? 8 / pairs : -1;
-  if (want >= 0)
-    while (p % 8 != want) ++p;
-  return p;
-}
 
 __device__ __forceinline__ uint64_t globaltimer() {
   uint64_t t;
@@ -118,17 +109,17 @@ __device__ __forceinline__ int wait_count(const int *p, int need, int *err) {
   }
 }
 
-__device__ __forceinline__ float4 ld_x(const float4 *p, uint64_t pol) {
-  float4 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "l"(p), "l"(pol));
-  return v;
+// evict-last L2 policy: the intermediate stays in L2 between the phases
+__device__ __forceinline__ uint64_t keep_policy() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
 }
-__device__ __forceinline__ void st_x(float4 *p, float4 v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y),
-               "f"(v.z), "f"(v.w), "l"(pol)
-               : "memory");
+__device__ __forceinline__ void st_keep(float2 *p, float2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_out(float2 *p, float2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol) : "memory");
 }
 __device__ __forceinline__ void discard_l2(const void *p) {
   asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
@@ -136,12 +127,79 @@ __device__ __forceinline__ void discard_l2(const void *p) {
 
 }  // namespace lg
 
+// Shared-memory wavefronts (8-byte slots, 16 per 128-byte wavefront) of the lanes of warp w over
+// one tile phase whose M lines of length 2^E sit `pitch` slots apart: the first pass's writes,
+// every middle pass's reads and writes and the last pass's reads, each with its lane-to-(line,
+// position) mapping. `across`: the first and last passes run lanes across the lines first (phase
+// A: the columns; phase B: only its last pass).
+namespace lg {
+constexpr int wave(const int (&slot)[32]) {
+  int cnt[16] = {}, worst = 0;
+  for (int l = 0; l < 32; ++l) {
+    const int b = slot[l] & 15;
+    if (++cnt[b] > worst) worst = cnt[b];
+  }
+  return worst;
+}
+constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side) {
+  const int L = 1 << E, NP = fx::np_of(E);
+  int total = 0;
+  for (int w = 0; w < NT / 32 && w < 4; ++w) {
+    int slot[32] = {};
+    // first pass (radix 16, output position 16 j + k)
+    for (int k = 0; k < 16; ++k) {
+      for (int l = 0; l < 32; ++l) {
+        const int u = 32 * w + l;
+        const int line = a_side ? u % M : u / (L / 16), j = a_side ? u / M : u % (L / 16);
+        slot[l] = line * pitch + sp(16 * j + k);
+      }
+      total += wave(slot);
+    }
+    for (int p = 1; p < NP; ++p) {
+      const int R = fx::radix_of(E, p), LR = L / R, NS = fx::ns_of(E, p);
+      for (int it = 0; it < (M * LR) / NT; ++it)
+        for (int k = 0; k < R; ++k) {
+          for (int l = 0; l < 32; ++l) {  // reads
+            const int u = 32 * w + l + it * NT;
+            const bool last = p == NP - 1;
+            const int line = last ? u % M : u / LR, j = last ? u / M : u % LR;
+            slot[l] = line * pitch + sp(j + k * LR);
+          }
+          total += wave(slot);
+          if (p < NP - 1) {
+            for (int l = 0; l < 32; ++l) {  // writes of a middle pass
+              const int u = 32 * w + l + it * NT;
+              const int line = u / LR, j = u % LR, m = j & (NS - 1);
+              slot[l] = line * pitch + sp((j - m) * R + m + k * NS);
+            }
+            total += wave(slot);
+          }
+        }
+    }
+  }
+  return total;
+}
+// The pitch (>= the padded line length, within 16 slots of it) with the fewest wavefronts.
+constexpr int best_pitch(int E, int M, int NT, bool a_side) {
+  const int base = sp((1 << E) - 1) + 1;
+  int best = base, cost = 1 << 30;
+  for (int p = base; p < base + 16; ++p) {
+    const int c = phase_waves(E, M, NT, p, a_side);
+    if (c < cost) {
+      cost = c;
+      best = p;
+    }
+  }
+  return best;
+}
+}  // namespace lg
+
 // Compile-time geometry: n1 = 2^E1 (phase-A length), n2 = 2^E2, tile of TT = 2^ET elements.
 template <int E1, int E2, int ET> struct LgCfg {
   static constexpr int N1 = 1 << E1, N2 = 1 << E2, TT = 1 << ET;
   static constexpr int C = TT / N1, D = TT / N2;  // columns per A tile, rows per B tile
-  static constexpr int NT = TT / 32;              // threads: one pair of radix-16 butterflies each
-  static constexpr int PA = lg::pitch(N1, C / 2), PB = lg::pitch(N2, D / 2);
+  static constexpr int NT = TT / 16;              // threads: one radix-16 butterfly each
+  static constexpr int PA = lg::best_pitch(E1, C, NT, true), PB = lg::best_pitch(E2, D, NT, false);
   static constexpr int SLOTS = C * PA > D * PB ? C * PA : D * PB;
   // the tile, then two control words (ticket, wait failure): no static shared memory, so the
   // dynamic size may be raised to the device's opt-in maximum
@@ -194,32 +252,23 @@ __device__ __forceinline__ void lg_middles(float2 *sm, const float2 *__restrict_
   }
 }
 
-// Last-pass butterfly j of the line pair (l0, l0 + 1): inputs from shared memory, twiddled,
-// transformed; output k lands at position j + k * NS of the transform.
+// Last-pass butterfly j of line l: inputs from shared memory, twiddled, transformed; output k
+// lands at position j + k * NS of the transform.
 template <int E, int PITCH>
-__device__ __forceinline__ void lg_last_pair(const float2 *sm, const float2 *__restrict__ tw, int l0, int j,
-                                             float2 (&a)[fx::radix_of(E, fx::np_of(E) - 1)],
-                                             float2 (&b)[fx::radix_of(E, fx::np_of(E) - 1)]) {
+__device__ __forceinline__ void lg_last_one(const float2 *sm, const float2 *__restrict__ tw, int l, int j,
+                                            float2 (&a)[fx::radix_of(E, fx::np_of(E) - 1)]) {
   constexpr int L = 1 << E, P = fx::np_of(E) - 1, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P);
   constexpr int TWO = fx::tw_of(E, P);
   static_assert(NS == LR, "last pass");
-  const float2 *s0 = sm + l0 * PITCH, *s1 = s0 + PITCH;
+  const float2 *s0 = sm + l * PITCH;
 #pragma unroll
-  for (int k = 0; k < R; ++k) {
-    a[k] = s0[lg::sp(j + k * LR)];
-    b[k] = s1[lg::sp(j + k * LR)];
-  }
+  for (int k = 0; k < R; ++k) a[k] = s0[lg::sp(j + k * LR)];
   if constexpr (NS > 1) {
     const float2 *t = tw + TWO + j;
 #pragma unroll
-    for (int k = 1; k < R; ++k) {
-      const float2 w = __ldg(t + (k - 1) * NS);
-      a[k] = mul<float>(a[k], w);
-      b[k] = mul<float>(b[k], w);
-    }
+    for (int k = 1; k < R; ++k) a[k] = mul<float>(a[k], __ldg(t + (k - 1) * NS));
   }
   dft<float, R>(a);
-  dft<float, R>(b);
 }
 
 // ---- paired lines of the real transforms ----
@@ -270,35 +319,27 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
                                            float2 *__restrict__ y, int part) {
   using Cf = LgCfg<E1, E2, ET>;
   constexpr int N1 = Cf::N1, N2 = Cf::N2, C = Cf::C, NT = Cf::NT, PA = Cf::PA;
-  constexpr int CP = C / 2;
   const float2 *tw = reinterpret_cast<const float2 *>(a.twA);
   if constexpr (KIND != LG_C2R) {
-    // first pass: radix 16 straight from global memory, two columns per 16-byte load
-    constexpr int R = 16, LR = N1 / R, UNITS = CP * LR;
+    // first pass: radix 16 straight from global memory; lanes run across the C columns first
+    constexpr int R = 16, LR = N1 / R, UNITS = C * LR;
     static_assert(UNITS == NT, "one unit per thread");
     const int u = int(threadIdx.x);
-    const int cp = u % CP, j = u / CP;
+    const int c = u % C, j = u / C;
     const uint64_t pol = input_policy(true);
-    const float4 *p = reinterpret_cast<const float4 *>(x + part * C + int64_t(j) * N2 + 2 * cp);
-    constexpr int64_t STEP = int64_t(LR) * N2 / 2;
-    float2 va[R], vb[R];
-    float4 q[R];
+    const float2 *p = x + part * C + int64_t(j) * N2 + c;
+    constexpr int64_t STEP = int64_t(LR) * N2;
+    float2 v[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) q[k] = lg::ld_x(p + k * STEP, pol);
-    const float sgn = a.conj_in ? -1.f : 1.f;
+    for (int k = 0; k < R; ++k) v[k] = ld_in(p + k * STEP, pol);
+    if (a.conj_in) {
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      va[k] = make_float2(q[k].x, q[k].y * sgn);
-      vb[k] = make_float2(q[k].z, q[k].w * sgn);
+      for (int k = 0; k < R; ++k) v[k].y = -v[k].y;
     }
-    dft<float, R>(va);
-    dft<float, R>(vb);
-    float2 *l0 = sm + (2 * cp) * PA, *l1 = l0 + PA;
+    dft<float, R>(v);
+    float2 *l0 = sm + c * PA;
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      l0[lg::sp(j * R + k)] = va[k];
-      l1[lg::sp(j * R + k)] = vb[k];
-    }
+    for (int k = 0; k < R; ++k) l0[lg::sp(j * R + k)] = v[k];
     __syncthreads();
     lg_middles<E1, C, NT, PA, 1, fx::np_of(E1) - 1>(sm, tw);
   } else {
@@ -338,39 +379,27 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     __syncthreads();
     lg_middles<E1, C, NT, PA, 0, fx::np_of(E1) - 1>(sm, tw);
   }
-  // last pass: outputs k1 = j + k * NS, times W_n^{j2 k1}, to Y[k1][j2]
+  // last pass: outputs k1 = j + k * NS, times W_n^{j2 k1}, to Y[k1][j2]; lanes across the C
+  // columns first (L2-resident stores, kept there with an evict-last policy)
   {
     constexpr int P = fx::np_of(E1) - 1, R = fx::radix_of(E1, P), LR = N1 / R, NS = LR;
-    constexpr int UNITS = CP * LR, ITER = UNITS / NT;
+    constexpr int UNITS = C * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
     const float2 *lo = reinterpret_cast<const float2 *>(a.lo), *hi = reinterpret_cast<const float2 *>(a.hi);
+    const uint64_t keep = lg::keep_policy();
 #pragma unroll
     for (int it = 0; it < ITER; ++it) {
       const int u = int(threadIdx.x) + it * NT;
-      const int cp = u % CP, j = u / CP;
-      float2 va[R], vb[R];
-      lg_last_pair<E1, PA>(sm, tw, 2 * cp, j, va, vb);
-      if constexpr (KIND != LG_C2R) {
-        // two adjacent columns per 16-byte store
-        const uint32_t c0 = uint32_t(part * C + 2 * cp);
-        float2 *yc = y + part * C + 2 * cp;
+      const int c = u % C, j = u / C;
+      float2 v[R];
+      lg_last_one<E1, PA>(sm, tw, c, j, v);
+      const int col = KIND == LG_C2R ? pair_index<N2, C>(part, c) : part * C + c;
+      float2 *yc = y + col;
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-          const uint32_t k1 = uint32_t(j + k * NS);
-          const float2 wa = split_twiddle<float>(lo, hi, a.shift, c0 * k1);
-          const float2 wb = split_twiddle<float>(lo, hi, a.shift, c0 * k1 + k1);
-          const float2 ra = mul<float>(va[k], wa), rb = mul<float>(vb[k], wb);
-          __stcg(reinterpret_cast<float4 *>(yc + int64_t(k1) * N2), make_float4(ra.x, ra.y, rb.x, rb.y));
-        }
-      } else {
-        // paired columns need not be adjacent: one 8-byte store per column
-        const uint32_t ca = uint32_t(pair_index<N2, C>(part, 2 * cp)), cb = uint32_t(pair_index<N2, C>(part, 2 * cp + 1));
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          const uint32_t k1 = uint32_t(j + k * NS);
-          __stcg(y + int64_t(k1) * N2 + ca, mul<float>(va[k], split_twiddle<float>(lo, hi, a.shift, ca * k1)));
-          __stcg(y + int64_t(k1) * N2 + cb, mul<float>(vb[k], split_twiddle<float>(lo, hi, a.shift, cb * k1)));
-        }
+      for (int k = 0; k < R; ++k) {
+        const uint32_t k1 = uint32_t(j + k * NS);
+        const float2 r = mul<float>(v[k], split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * k1));
+        lg::st_keep(yc + int64_t(k1) * N2, r, keep);
       }
     }
   }
@@ -389,31 +418,20 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     const int k1 = KIND == LG_R2C ? pair_index<N1, D>(part, r) : part * D + r;
     return yg + int64_t(k1) * N2;
   };
-  // first pass: radix 16 from Y (L2), two adjacent butterflies per 16-byte load
+  // first pass: radix 16 from Y (L2); lanes along the row
   {
-    constexpr int R = 16, LR = N2 / R, JP = LR / 2, UNITS = D * JP;
+    constexpr int R = 16, LR = N2 / R, UNITS = D * LR;
     static_assert(UNITS == NT, "one unit per thread");
     const int u = int(threadIdx.x);
-    const int r = u / JP, jp = u % JP;
-    const float4 *p = reinterpret_cast<const float4 *>(yrow(r) + 2 * jp);
-    float4 q[R];
+    const int r = u / LR, j = u % LR;
+    const float2 *p = yrow(r) + j;
+    float2 v[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) q[k] = __ldcg(p + k * (LR / 2));
-    float2 va[R], vb[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      va[k] = make_float2(q[k].x, q[k].y);
-      vb[k] = make_float2(q[k].z, q[k].w);
-    }
-    dft<float, R>(va);
-    dft<float, R>(vb);
+    for (int k = 0; k < R; ++k) v[k] = __ldcg(p + k * LR);
+    dft<float, R>(v);
     float2 *l = sm + r * PB;
-    const int j0 = 2 * jp;
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      l[lg::sp(j0 * R + k)] = va[k];
-      l[lg::sp((j0 + 1) * R + k)] = vb[k];
-    }
+    for (int k = 0; k < R; ++k) l[lg::sp(j * R + k)] = v[k];
   }
   __syncthreads();
   if (a.flags & kLongDiscard) {
@@ -427,22 +445,21 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
   const uint64_t pol = input_policy((a.flags & kLongEvictOut) != 0);
   if constexpr (KIND != LG_R2C) {
     lg_middles<E2, D, NT, PB, 1, fx::np_of(E2) - 1>(sm, tw);
-    // last pass: outputs k2 = j + k * NS of rows (2rp, 2rp + 1) to X[2rp + k2 n1] (16-byte stores)
+    // last pass: outputs k2 = j + k * NS of row r to X[r + k2 n1]; lanes across the D rows first
     constexpr int P = fx::np_of(E2) - 1, R = fx::radix_of(E2, P), LR = N2 / R, NS = LR;
-    constexpr int RP = D / 2, UNITS = RP * LR, ITER = UNITS / NT;
+    constexpr int UNITS = D * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
     float2 *Xt = X + part * D;
 #pragma unroll
     for (int it = 0; it < ITER; ++it) {
       const int u = int(threadIdx.x) + it * NT;
-      const int rp = u % RP, j = u / RP;
-      float2 va[R], vb[R];
-      lg_last_pair<E2, PB>(sm, tw, 2 * rp, j, va, vb);
+      const int r = u % D, j = u / D;
+      float2 v[R];
+      lg_last_one<E2, PB>(sm, tw, r, j, v);
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const int64_t k2 = j + k * NS;
-        lg::st_x(reinterpret_cast<float4 *>(Xt + 2 * rp + k2 * N1),
-                 make_float4(va[k].x * fct, va[k].y * sgn, vb[k].x * fct, vb[k].y * sgn), pol);
+        lg::st_out(Xt + r + k2 * N1, make_float2(v[k].x * fct, v[k].y * sgn), pol);
       }
     }
   } else {
@@ -477,30 +494,29 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
 
 // ---- the persistent kernel ----
 
-// Ticket block -> (group, phase).
+// Ticket block -> (group, phase), for lookahead `look` (0 <= look <= ng).
 __device__ __forceinline__ void lg_decode(int blk, int ng, int look, int &g, bool &isA) {
-  if (look == 0) {
-    g = blk >> 1;
-    isA = (blk & 1) == 0;
-  } else if (blk == 0) {
-    g = 0;
+  if (blk < look) {
+    g = blk;
     isA = true;
-  } else if (blk == 2 * ng - 1) {
-    g = ng - 1;
-    isA = false;
-  } else if (blk & 1) {
-    g = (blk + 1) >> 1;
-    isA = true;
+  } else if (blk < 2 * ng - look) {
+    const int k = blk - look;
+    isA = (k & 1) == 0;
+    g = isA ? look + (k >> 1) : (k >> 1);
   } else {
-    g = (blk >> 1) - 1;
+    g = blk - ng;
     isA = false;
   }
+}
+
+__device__ __forceinline__ void red_release_add(int *p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // KIND: LG_C2C (complex in, complex out), LG_R2C (real in, n/2+1 complex out), LG_C2R. Row
 // offsets from the sides are in units of the side's element (float for real rows).
 template <int KIND, int E1, int E2, int ET>
-__global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, 512 / LgCfg<E1, E2, ET>::NT)
+__global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, 1024 / LgCfg<E1, E2, ET>::NT)
     long_kernel(const __grid_constant__ LongArgs a) {
   using Cf = LgCfg<E1, E2, ET>;
   constexpr int64_t n = int64_t(1) << (E1 + E2);
@@ -515,8 +531,13 @@ __global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, 512 / LgCfg<E1, E2, ET>
   const int N = a.tiles;
   const int total = 2 * a.ngroups * N;
   int *doneA = a.ctr + 3, *doneB = a.ctr + 3 + a.ngroups;
+  int next = 0;  // thread 0: the ticket after the current one, taken while the current one runs
+  if (threadIdx.x == 0) next = atomicAdd(a.ctr, 1);
   for (;;) {
-    if (threadIdx.x == 0) s_t = atomicAdd(a.ctr, 1);
+    if (threadIdx.x == 0) {
+      s_t = next;
+      if (next < total) next = atomicAdd(a.ctr, 1);
+    }
     __syncthreads();
     const int t = s_t;
     if (t >= total) break;
@@ -559,10 +580,8 @@ __global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, 512 / LgCfg<E1, E2, ET>
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(isA ? doneA + g : doneB + g, 1);
-    }
+    // every thread's stores of this tile precede the count (barrier, then a release reduction)
+    if (threadIdx.x == 0) red_release_add(isA ? doneA + g : doneB + g, 1);
   }
 }
 

@@ -1,0 +1,13 @@
+// Instances of the long-transform kernel for kind LG_C2C (rg_long.cuh, rg_long_launch.cuh).
+#include "rg_long_launch.cuh"
+
+namespace rg {
+
+template <> bool long_dispatch<LG_C2C>(int e1, int e2, int et, LongArgs &a, int64_t tickets, cudaStream_t st) {
+  constexpr int KIND_ = LG_C2C;
+  RG_LONG_SHAPES(RG_LONG_CASE)
+  RG_LONG_SHAPES_C2C_ONLY(RG_LONG_CASE)
+  return false;
+}
+
+}  // namespace rg

@@ -457,7 +457,7 @@ def tc_error(stream=None):
 
 
 def tc_selftest(A, A2, B, B2, D):
-    """D = A B^T + A B2^T + A2 B^T + A2 B2^T on the tensor cores (device torch tensors: A, A2 float16
+    """D = A B^T + A B2^T + A2 B^T on the tensor cores (device torch tensors: A, A2 float16
     256 x 32, B, B2 float16 32 x 32, D float32 256 x 32, all contiguous), through the operand
     layout and tensor-memory path of the transform kernels. Runs on the current torch stream."""
     import torch

@@ -172,3 +172,30 @@ def test_long_real_flags_rings_strides(rg, cuda, nbuf, monkeypatch):
     assert rg.long_error() == 0
     assert oracle.rel_l2(out[:, :n].cpu().numpy(), _oracle_c2r(Xh, n, True, 2.0 / n)) <= 1e-6
     assert float(out[:, n:].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("shift", ["-1", "-2"])
+@pytest.mark.parametrize("e,rows", [(14, 40), (16, 11), (18, 5), (20, 3), (22, 2)])
+def test_long_smaller_tiles(rg, cuda, e, rows, shift, monkeypatch):
+    """The smaller-tile instances (ROCKET_GPU_LONG_ET_SHIFT: half or a quarter of the default
+    tile, more CTAs per SM): c2c, and r2c / c2r of 2n points, against the oracle."""
+    torch = cuda
+    monkeypatch.setenv("ROCKET_GPU_LONG_ET_SHIFT", shift)
+    n = 1 << e
+    rng = np.random.default_rng(120 + e)
+    ax = np.array([1], np.int64)
+    x = (rng.standard_normal((rows, n)) + 1j * rng.standard_normal((rows, n))).astype(np.complex64)
+    xd = torch.from_numpy(x).cuda()
+    X = torch.empty_like(xd)
+    rg.c2c(xd, X, ax, True, 1.0, 1)
+    assert rg.long_error() == 0
+    assert oracle.rel_l2(X.cpu().numpy(), _oracle_c2c(x, True, 1.0)) <= 1e-6
+    if e < 24:
+        r = rng.standard_normal((rows, 2 * n)).astype(np.float32)
+        R = torch.empty((rows, n + 1), dtype=torch.complex64, device="cuda")
+        rg.r2c(torch.from_numpy(r).cuda(), R, ax, True, 1.0, 1)
+        assert oracle.rel_l2(R.cpu().numpy(), _oracle_r2c(r, True, 1.0)) <= 1e-6
+        back = torch.empty((rows, 2 * n), dtype=torch.float32, device="cuda")
+        rg.c2r(R, back, ax, False, 1.0 / (2 * n), 1)
+        assert rg.long_error() == 0
+        assert oracle.rel_l2(back.cpu().numpy(), r) <= 2e-6
