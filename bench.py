@@ -41,8 +41,10 @@ METRIC = "transforms/s"
 WORKLOAD = "3-D r2c + c2r round trip, float32 256x256x256, axes [0,1,2], fct 1 and 1/256^3"
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant
-# kernel from one `ncu --set full` capture of this workload (GB300, cold caches): 67.65 MB read
-# + 7.30 MB written; most of the 67.6 MB output is still dirty in L2 when the launch ends.
+# kernel of the default workload (the 256^3 round trip) from one `ncu --set full` capture
+# (GB300, cold caches): 67.65 MB read + 7.30 MB written; most of the 67.6 MB output is still
+# dirty in L2 when the launch ends. Only the default line uses it (the other workloads' kernels
+# of the same name run other lengths).
 NCU_TRAFFIC = {"axis_c2c_f32": 67_653_632 + 7_301_376}
 
 
@@ -228,7 +230,7 @@ def kernel_profile(step, steps):
     achieved = dom["bytes"] / dom["launches"] / (dom["total_ms"] / dom["launches"] / 1e3) / 1e9
     peak, peak_kind = peaks()
     roof = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": NCU_TRAFFIC.get(dom["name"]),
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
             "launch_ms": dom["total_ms"] / dom["launches"], "bytes_per_launch": dom["bytes"] // dom["launches"],
             "share": dom["total_ms"] / total_ms}
     kernels = [{"name": s["name"], "launches": s["launches"], "ms": s["total_ms"], "share": s["total_ms"] / total_ms,
