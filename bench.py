@@ -279,6 +279,51 @@ def c1_form(torch, rg, steps):
             "unit": "transforms/s", "ms_per_step": ms, "roofline_fp64": fp64_roofline(rg, ms)}
 
 
+def c3_form(torch, rg, steps):
+    """The uneven batch (10,000 complex64 lengths) in one autotuned persistent launch replayed
+    from a CUDA graph, against per-transform c2c calls of the same rows (host-issued: the
+    per-launch arm includes the Python issue cost of 10,000 calls), for the default line's forms."""
+    import importlib
+
+    batch = importlib.import_module("rocket_fft_gb300.batch")
+    lengths = batch.c3_lengths(10000, seed=0)
+    t0 = time.perf_counter()
+    plan = batch.BatchedC2C(lengths, dtype=torch.complex64, forward=True, fct=1.0, autotune=True)
+    plan_s = time.perf_counter() - t0
+    gen = torch.Generator(device="cuda").manual_seed(13)
+    x = torch.complex(torch.randn(plan.total, device="cuda", generator=gen),
+                      torch.randn(plan.total, device="cuda", generator=gen))
+    y = torch.empty_like(x)
+    plan.graph(x, y)
+    for _ in range(3):
+        plan.replay()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        plan.replay()
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    axes = np.array([0], dtype=np.int64)
+    yp = torch.empty_like(x)
+    rows = [(int(o), int(n)) for o, n in zip(plan.offsets, plan.lengths)]
+    for o, n in rows:  # plans warm
+        rg.c2c(x[o:o + n], yp[o:o + n], axes, True, 1.0, 1)
+    torch.cuda.synchronize()
+    a.record()
+    for o, n in rows:
+        rg.c2c(x[o:o + n], yp[o:o + n], axes, True, 1.0, 1)
+    b.record()
+    b.synchronize()
+    per_ms = a.elapsed_time(b)
+    return {"workload": "10,000 complex64 c2c of uneven lengths (40% 7-smooth, 20% primes, 40% uniform in "
+                        "[16, 65536]), one persistent launch from a CUDA graph", "value": len(rows) / (ms / 1e3),
+            "unit": "transforms/s", "ms_per_batch": ms, "per_launch_ms": per_ms, "vs_per_launch": per_ms / ms,
+            "per_launch_note": "10,000 host-issued c2c calls, device time between events: includes issue cost",
+            "planning_s_incl_autotune": plan_s}
+
+
 def run_c1(args):
     """Config 1: c2c complex128, batch 256 x length 4096, axes [1], forward, fct 1."""
     import torch
@@ -782,6 +827,8 @@ def run_ours(args):
 
     # complex128 (config 1) beside it: rate and FP64 roofline
     c1 = c1_form(torch, rg, args.steps) if rank == 0 else None
+    # the uneven batch (config 3): batched against per-transform launches
+    c3 = c3_form(torch, rg, args.steps) if rank == 0 else None
 
     # e2e: the same round trip through the C ABI on pinned host arrays
     e2e = None
@@ -837,7 +884,7 @@ def run_ours(args):
             "accuracy": acc,
             "forms": {"plain_fp32": {"value": value, "ms_per_step": ms / args.steps,
                                      "r2c_rel_l2_vs_fp64": acc.get("r2c_rel_l2_vs_fp64")},
-                      "tc_split_fp16": tc_form, "complex128_c1": c1},
+                      "tc_split_fp16": tc_form, "complex128_c1": c1, "batched_c3": c3},
             "length_range": length_range,
             "cpu_baseline": cpu,
             "e2e": e2e,
