@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -455,12 +456,24 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
   struct Cand {
     int Lmax, threads, policy;
   };
-  std::vector<Cand> cands = {{4096, 256, 0}};
+  // on-chip capacities whose two shared row buffers fit a CTA (8192: one CTA per SM, single
+  // precision only); without the autotune, ROCKET_GPU_BATCH_LMAX picks one (default 4096)
+  auto fits = [&](int Lmax) {
+    int pitch = 0, ps = 0;
+    return pitch_bytes(dt, Lmax, pitch, ps) <= max_smem_optin();
+  };
+  int lmax0 = 4096;
+  if (const char *e = std::getenv("ROCKET_GPU_BATCH_LMAX")) {
+    const int v = std::atoi(e);
+    if ((v == 2048 || v == 4096 || v == 8192) && fits(v)) lmax0 = v;
+  }
+  std::vector<Cand> cands = {{lmax0, 256, 0}};
   if (autotune) {
     cands.clear();
-    for (int Lmax : {2048, 4096})
-      for (int th : {256, 512})
-        for (int pol : {0, 1}) cands.push_back({Lmax, th, pol});
+    for (int Lmax : {2048, 4096, 8192})
+      if (fits(Lmax))
+        for (int th : {256, 512})
+          for (int pol : {0, 1}) cands.push_back({Lmax, th, pol});
   }
   if (cands.size() == 1) {
     build(*p, cands[0].Lmax, cands[0].threads, cands[0].policy);

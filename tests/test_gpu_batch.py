@@ -17,10 +17,14 @@ pytestmark = pytest.mark.gpu
 LENGTHS = [16, 17, 100, 127, 1000, 4096, 4099, 5000, 8192, 12289, 25600, 65536, 65521, 3, 1, 2, 4097, 30030]
 
 
+@pytest.mark.parametrize("lmax", ["2048", "4096", "8192"])
 @pytest.mark.parametrize("dtype", ["complex64", "complex128"])
 @pytest.mark.parametrize("forward", [True, False])
-def test_batch_matches_per_row(rg, cuda, dtype, forward):
+def test_batch_matches_per_row(rg, cuda, dtype, forward, lmax, monkeypatch):
+    """Each on-chip capacity (ROCKET_GPU_BATCH_LMAX; 8192 is single precision only, complex128
+    keeps 4096)."""
     torch = cuda
+    monkeypatch.setenv("ROCKET_GPU_BATCH_LMAX", lmax)
     batch = importlib.import_module("rocket_fft_gb300.batch")
     tdt = getattr(torch, dtype)
     plan = batch.BatchedC2C(LENGTHS, dtype=tdt, forward=forward, fct=0.5, autotune=False)
