@@ -77,6 +77,16 @@ namespace lg {
 // shared index of position pos of a line: one pad slot per 32 positions
 __host__ __device__ constexpr int sp(int pos) { return pos + (pos >> 5); }
 
+// sp(base + k * STEP) as the base's index plus a compile-time offset, for the runs the passes
+// use: STEP a multiple of 32 (any base), STEP 16 with base % 32 < 16, STEP 1 with
+// base % 32 + k < 32 (checked for every access of every instantiated length); else sp().
+template <int STEP> __device__ __forceinline__ int sp_k(int base, int k) {
+  if constexpr (STEP % 32 == 0) return base + (base >> 5) + k * (STEP + STEP / 32);
+  else if constexpr (STEP == 16) return base + (base >> 5) + 16 * k + (k >> 1);
+  else if constexpr (STEP == 1) return base + (base >> 5) + k;
+  else return sp(base + k * STEP);
+}
+
 __device__ __forceinline__ uint64_t globaltimer() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -223,7 +233,7 @@ __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__
     const int line = u / LR, j = u % LR;
     const float2 *s = sm + line * PITCH;
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[it][k] = s[lg::sp(j + k * LR)];
+    for (int k = 0; k < R; ++k) v[it][k] = s[lg::sp_k<LR>(j, k)];
     if constexpr (NS > 1) {
       const float2 *t = tw + TWO + (j & (NS - 1));
 #pragma unroll
@@ -239,7 +249,7 @@ __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__
     const int m = j & (NS - 1), base = (j - m) * R + m;
     float2 *s = sm + line * PITCH;
 #pragma unroll
-    for (int k = 0; k < R; ++k) s[lg::sp(base + k * NS)] = v[it][k];
+    for (int k = 0; k < R; ++k) s[lg::sp_k<NS>(base, k)] = v[it][k];
   }
   __syncthreads();
 }
@@ -262,7 +272,7 @@ __device__ __forceinline__ void lg_last_one(const float2 *sm, const float2 *__re
   static_assert(NS == LR, "last pass");
   const float2 *s0 = sm + l * PITCH;
 #pragma unroll
-  for (int k = 0; k < R; ++k) a[k] = s0[lg::sp(j + k * LR)];
+  for (int k = 0; k < R; ++k) a[k] = s0[lg::sp_k<LR>(j, k)];
   if constexpr (NS > 1) {
     const float2 *t = tw + TWO + j;
 #pragma unroll
@@ -339,7 +349,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     dft<float, R>(v);
     float2 *l0 = sm + c * PA;
 #pragma unroll
-    for (int k = 0; k < R; ++k) l0[lg::sp(j * R + k)] = v[k];
+    for (int k = 0; k < R; ++k) l0[lg::sp_k<1>(j * R, k)] = v[k];
     __syncthreads();
     lg_middles<E1, C, NT, PA, 1, fx::np_of(E1) - 1>(sm, tw);
   } else {
@@ -431,7 +441,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     dft<float, R>(v);
     float2 *l = sm + r * PB;
 #pragma unroll
-    for (int k = 0; k < R; ++k) l[lg::sp(j * R + k)] = v[k];
+    for (int k = 0; k < R; ++k) l[lg::sp_k<1>(j * R, k)] = v[k];
   }
   __syncthreads();
   if (a.flags & kLongDiscard) {
