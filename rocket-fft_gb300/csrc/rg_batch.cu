@@ -122,7 +122,8 @@ template <typename T> struct K {
   __device__ cx<T> *fft(int rows, const FFTCore &core) { return fft_rows<T>(s0, s1, rows, pitch, a.ps, core); }
 
   // rows x len from shared `res` to global (row r at base + r*rstride + i*estride); optional
-  // four-step twiddle W_N^{(col0 + r) * i}; optional conj/fct; optional *bk (y = conj(F*bk)).
+  // four-step twiddle W_N^{(col0 + r) * i}; optional conj/fct; optional *bk (y = conj(F*bk), bk
+  // indexed like the output: bk[r*rstride + i*estride]).
   // colwalk: consecutive threads take consecutive rows (rows adjacent in memory, rstride 1).
   __device__ void store(const cx<T> *res, cx<T> *base, int rows, int len, int64_t rstride, int64_t estride,
                         bool conj_out, T scale, const cx<T> *lo = nullptr, const cx<T> *hi = nullptr, int shift = 0,
@@ -140,17 +141,19 @@ template <typename T> struct K {
       if (i >= nvalid) continue;
       cx<T> v = res[sidx(r, i, pitch, a.ps)];
       if (lo) v = mul<T>(v, split_twiddle<T>(lo, hi, shift, uint32_t(col0 + r) * uint32_t(i)));
-      if (bk) v = cj<T>(mul<T>(v, bk[i]));
+      if (bk) v = cj<T>(mul<T>(v, bk[r * rstride + i * estride]));
       v = mk<T>(v.x * scale, (conj_out ? -v.y : v.y) * scale);
       base[r * rstride + i * estride] = v;
     }
     __syncthreads();
   }
 
-  // dst = DFT_n(src) for n = n1 * n2 through `tmp` (column pass, then row pass)
+  // dst = DFT_n(src) for n = n1 * n2 through `tmp` (column pass, then row pass); with bk_out the
+  // row pass stores conj(DFT * bk_out) (the Bluestein spectrum product, fused into the store)
   __device__ void four_step(const cx<T> *src, cx<T> *dst, cx<T> *tmp, int n1, int n2, const FFTCore &c1,
                             const FFTCore &c2, const cx<T> *lo, const cx<T> *hi, int shift, bool conj_in,
-                            bool conj_out, T scale, const cx<T> *bk_in = nullptr, int nvalid_in = 1 << 30) {
+                            bool conj_out, T scale, const cx<T> *bk_in = nullptr, int nvalid_in = 1 << 30,
+                            const cx<T> *bk_out = nullptr) {
     const int64_t n = int64_t(n1) * n2;
     (void)n;
     const int tbA = rows_for(n1);
@@ -197,7 +200,8 @@ template <typename T> struct K {
       const int rows = min(tbB, n1 - k0);
       load(tmp + int64_t(k0) * n2, rows, n2, n2, 1, false);
       cx<T> *res = fft(rows, c2);
-      store(res, dst + k0, rows, n2, 1, n1, conj_out, scale, nullptr, nullptr, 0, 0, nullptr, 1 << 30, true);
+      store(res, dst + k0, rows, n2, 1, n1, conj_out, scale, nullptr, nullptr, 0, 0, bk_out ? bk_out + k0 : nullptr,
+            1 << 30, true);
     }
   }
 };
@@ -249,10 +253,9 @@ __global__ void __launch_bounds__(512) batch_kernel(const __grid_constant__ Batc
       k.store(res, y, 1, I.n, 0, 1, k.bwd, k.fct, nullptr, nullptr, 0, 0, bk, I.n);
     } else {  // IT_BLUE_FOUR: workspace w holds 2m elements (A, B)
       cx<T> *A = w, *B = w + I.m;
-      k.four_step(x, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, k.bwd, false, T(1), bk, I.n);
-      __syncthreads();
-#pragma unroll 4
-      for (int i = threadIdx.x; i < I.m; i += blockDim.x) A[i] = cj<T>(mul<T>(A[i], bkf[i]));
+      // A = conj(FFT(x conj(bk)) * bkf): the spectrum product fused into the first FFT's store
+      k.four_step(x, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, k.bwd, false, T(1), bk, I.n,
+                  bkf);
       __syncthreads();
       k.four_step(A, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, false, false, T(1));
       __syncthreads();

@@ -199,3 +199,43 @@ def test_long_smaller_tiles(rg, cuda, e, rows, shift, monkeypatch):
         rg.c2r(R, back, ax, False, 1.0 / (2 * n), 1)
         assert rg.long_error() == 0
         assert oracle.rel_l2(back.cpu().numpy(), r) <= 2e-6
+
+
+@pytest.mark.parametrize("n", [1 << 15, 1 << 16, 3 * (1 << 14)])
+def test_long_lengths_through_other_transforms(rg, cuda, n):
+    """The other transform families at lengths whose real or complex sub-transforms take the long
+    kernel (or, for 3 * 2^14, the generic four-step route): DCT and DST of types 1-4, c2c_sym,
+    r2r_fftpack both ways and both Hartley forms, float32 and float64, against the oracle."""
+    torch = cuda
+    rng = np.random.default_rng(130)
+    P = oracle.port()
+    ax = np.array([1], np.int64)
+    for rdt, tol in ((np.float32, 1e-6), (np.float64, 1e-13)):
+        x = rng.standard_normal((3, n)).astype(rdt)
+        xd = torch.from_numpy(x).cuda()
+        x64 = x.astype(np.float64)
+        for kind in ("dct", "dst"):
+            for t in (1, 2, 3, 4):
+                y = torch.empty_like(xd)
+                getattr(rg, kind)(xd, y, ax, t, 1.0, False, 1)
+                want = np.empty_like(x64)
+                getattr(P, kind)(x64, want, [1], t, 1.0, False, 8)
+                assert oracle.rel_l2(y.cpu().numpy(), want) <= tol, (kind, t, n, rdt)
+        Y = torch.empty((3, n), dtype=torch.complex64 if rdt == np.float32 else torch.complex128, device="cuda")
+        rg.c2c_sym(xd, Y, ax, True, 1.0, 1)
+        want = np.empty((3, n), np.complex128)
+        P.c2c_sym(x64, want, [1], True, 1.0, 8)
+        assert oracle.rel_l2(Y.cpu().numpy(), want) <= tol, ("c2c_sym", n, rdt)
+        for r2h in (True, False):
+            y = torch.empty_like(xd)
+            rg.r2r_fftpack(xd, y, ax, r2h, r2h, 1.0, 1)
+            want = np.empty_like(x64)
+            P.r2r_fftpack(x64, want, [1], r2h, r2h, 1.0, 8)
+            assert oracle.rel_l2(y.cpu().numpy(), want) <= tol, ("fftpack", r2h, n, rdt)
+        for kind in ("r2r_separable_hartley", "r2r_genuine_hartley"):
+            y = torch.empty_like(xd)
+            getattr(rg, kind)(xd, y, ax, 1.0, 1)
+            want = np.empty_like(x64)
+            getattr(P, kind)(x64, want, [1], 1.0, 8)
+            assert oracle.rel_l2(y.cpu().numpy(), want) <= tol, (kind, n, rdt)
+    assert rg.long_error() == 0
