@@ -94,6 +94,13 @@ template <typename T, int OP, int E, bool COL> struct FxCfg {
   static constexpr int NT = fx::clampi(TB * L / 16, 64, 512);
   static constexpr int NBUF = OP == OP_C2C && NP == 1 ? 0 : 1;  // middle passes run in place
   static constexpr size_t SMEM = size_t(NBUF) * TB * PITCH * ESZ;
+  // CTAs per SM the register allocation leaves room for (float32): 48 registers a thread up to
+  // 256 threads, 64 at 512. Left to itself the allocator kept 54-128 registers for the ILP of the
+  // butterflies and the DCT pre/post steps, and the register file then held these memory-bound
+  // passes to 2-4 CTAs per SM. Measured on GB300 (256^3 / 512^3 inputs, L2-cold): r2c L=128 rows
+  // 36.5 -> 33.0 us, DCT-III half length 512^3 416 -> 278 us, batched r2c of 2^12 points 0.51 ->
+  // 0.65 of the HBM copy bandwidth; the slowest change was +2 % (a strided L=256 c2c pass).
+  static constexpr int MINB = sizeof(T) != 4 ? 1 : NT >= 512 ? 2 : NT == 256 ? 5 : NT == 128 ? 10 : 21;
   static_assert(NT % TB == 0 && NT / TB >= 1, "threads per row");
 };
 
@@ -469,7 +476,7 @@ __device__ __forceinline__ void fx_middle(const KArgs &a, uint32_t row0, int row
 }
 
 template <typename T, int OP, int E, bool COL, bool BWD>
-__global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT)
+__global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT, FxCfg<T, OP, E, COL>::MINB)
     fixed_kernel(const __grid_constant__ KArgs a, int pair_ok_i) {
   pdl_begin();
   using C = FxCfg<T, OP, E, COL>;
