@@ -10,8 +10,9 @@
 //              itself in two passes), chirp products and the spectrum product in between
 // Inputs and outputs are flat concatenations of the rows. The plan owns its tables and the
 // workspace (one region per item), so execution allocates nothing and can be captured in a CUDA
-// graph. Lmax, the threads per CTA and the four-step split policy are chosen by timing the
-// candidates on the plan's own lengths (rocketgpu_batch_create with autotune).
+// graph. Lmax, the threads and register budget per CTA and the four-step split policy are
+// chosen by timing the candidates on the plan's own lengths (rocketgpu_batch_create with
+// autotune).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -206,8 +207,14 @@ template <typename T> struct K {
   }
 };
 
-template <typename T>
-__global__ void __launch_bounds__(512) batch_kernel(const __grid_constant__ BatchArgs a) {
+// Register budgets of the kernel instances: V = 0 up to 512 threads at one CTA per SM (128
+// registers); V = 1 and 2 at 256 threads for 3 and 4 CTAs per SM (80 and 64 registers; single
+// precision only, double precision spills at those budgets). The autotuner picks one.
+constexpr int kBatchNT[3] = {512, 256, 256};
+constexpr int kBatchMinB[3] = {1, 3, 4};
+
+template <typename T, int V>
+__global__ void __launch_bounds__(kBatchNT[V], kBatchMinB[V]) batch_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_item;
   cx<T> *s0 = reinterpret_cast<cx<T> *>(smraw);
@@ -286,7 +293,7 @@ struct BatchPlan {
   std::vector<int64_t> lengths;
   int64_t total = 0;  // sum of lengths
   // chosen configuration
-  int Lmax = 4096, threads = 256, split = 0;
+  int Lmax = 4096, threads = 256, split = 0, variant = 0;
   std::string tune_log;
   // device state
   Item *d_items = nullptr;
@@ -336,12 +343,24 @@ double cost(const Item &I) {
   }
 }
 
+const void *kernel_fn(DType dt, int variant) {
+  if (dt != DType::F32) return reinterpret_cast<const void *>(&batch_kernel<double, 0>);
+  switch (variant) {
+    case 1: return reinterpret_cast<const void *>(&batch_kernel<float, 1>);
+    case 2: return reinterpret_cast<const void *>(&batch_kernel<float, 2>);
+    default: return reinterpret_cast<const void *>(&batch_kernel<float, 0>);
+  }
+}
+
 // Build items, cores and workspace for one configuration (device memory owned by `p`).
-void build(BatchPlan &p, int Lmax, int threads, int policy) {
+void build(BatchPlan &p, int Lmax, int threads, int policy, int variant) {
   const DType dt = p.dt;
+  RG_CHECK(variant >= 0 && variant < 3 && (variant == 0 || dt == DType::F32) && threads <= kBatchNT[variant],
+           RG_ERR_INTERNAL, "batch kernel variant");
   p.Lmax = Lmax;
   p.threads = threads;
   p.split = policy;
+  p.variant = variant;
   std::vector<Item> items;
   std::vector<FFTCore> cores;
   std::vector<int> core_len;
@@ -411,8 +430,7 @@ void build(BatchPlan &p, int Lmax, int threads, int policy) {
   int dev = 0, sms = 0;
   RG_CUDA(cudaGetDevice(&dev));
   RG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const void *fn = dt == DType::F32 ? reinterpret_cast<const void *>(&batch_kernel<float>)
-                                    : reinterpret_cast<const void *>(&batch_kernel<double>);
+  const void *fn = kernel_fn(dt, variant);
   RG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(p.smem)));
   int per_sm = 0;
   RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, p.smem));
@@ -437,10 +455,14 @@ void batch_exec(BatchPlan &p, const void *in, void *out, cudaStream_t st) {
   a.Lmax = p.Lmax;
   a.pitch = p.pitch;
   a.ps = p.ps;
-  if (p.dt == DType::F32)
-    batch_kernel<float><<<p.grid, p.threads, p.smem, st>>>(a);
+  if (p.dt != DType::F32)
+    batch_kernel<double, 0><<<p.grid, p.threads, p.smem, st>>>(a);
+  else if (p.variant == 1)
+    batch_kernel<float, 1><<<p.grid, p.threads, p.smem, st>>>(a);
+  else if (p.variant == 2)
+    batch_kernel<float, 2><<<p.grid, p.threads, p.smem, st>>>(a);
   else
-    batch_kernel<double><<<p.grid, p.threads, p.smem, st>>>(a);
+    batch_kernel<float, 0><<<p.grid, p.threads, p.smem, st>>>(a);
   note_launch();
   RG_CUDA(cudaGetLastError());
 }
@@ -457,7 +479,7 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
     p->total += lengths[i];
   }
   struct Cand {
-    int Lmax, threads, policy;
+    int Lmax, threads, policy, variant;
   };
   // on-chip capacities whose two shared row buffers fit a CTA (8192: one CTA per SM, single
   // precision only); without the autotune, ROCKET_GPU_BATCH_LMAX picks one (default 4096)
@@ -470,16 +492,29 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
     const int v = std::atoi(e);
     if ((v == 2048 || v == 4096 || v == 8192) && fits(v)) lmax0 = v;
   }
-  std::vector<Cand> cands = {{lmax0, 256, 0}};
+  // ROCKET_GPU_BATCH_CTAS (3 or 4, single precision) picks the 80- or 64-register instance
+  int var0 = 0;
+  if (const char *e = std::getenv("ROCKET_GPU_BATCH_CTAS")) {
+    const int v = std::atoi(e);
+    if (dt == DType::F32 && (v == 3 || v == 4)) var0 = v - 2;
+  }
+  std::vector<Cand> cands = {{lmax0, 256, 0, var0}};
   if (autotune) {
+    // every capacity x (threads, register budget) with the square-root split; then the other
+    // split policy for the fastest of those
     cands.clear();
     for (int Lmax : {2048, 4096, 8192})
-      if (fits(Lmax))
-        for (int th : {256, 512})
-          for (int pol : {0, 1}) cands.push_back({Lmax, th, pol});
+      if (fits(Lmax)) {
+        cands.push_back({Lmax, 256, 0, 0});
+        cands.push_back({Lmax, 512, 0, 0});
+        if (dt == DType::F32) {
+          cands.push_back({Lmax, 256, 0, 1});
+          cands.push_back({Lmax, 256, 0, 2});
+        }
+      }
   }
   if (cands.size() == 1) {
-    build(*p, cands[0].Lmax, cands[0].threads, cands[0].policy);
+    build(*p, cands[0].Lmax, cands[0].threads, cands[0].policy, cands[0].variant);
     return p.release();
   }
   // time every candidate on the plan's own lengths (random data, two runs each, best kept)
@@ -494,9 +529,11 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
   std::ostringstream log;
   float best = 1e30f;
   Cand pick = cands[0];
+  bool split_tried = false;
   try {
-    for (const Cand &c : cands) {
-      build(*p, c.Lmax, c.threads, c.policy);
+    for (size_t ci = 0; ci < cands.size(); ++ci) {
+      const Cand c = cands[ci];
+      build(*p, c.Lmax, c.threads, c.policy, c.variant);
       batch_exec(*p, din, dout, nullptr);  // warm-up
       float t = 1e30f;
       for (int rep = 0; rep < 2; ++rep) {
@@ -508,10 +545,15 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
         RG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         t = std::min(t, ms);
       }
-      log << "Lmax=" << c.Lmax << ",threads=" << c.threads << ",split=" << c.policy << ":" << t << "ms;";
+      log << "Lmax=" << c.Lmax << ",threads=" << c.threads << ",ctas=" << kBatchMinB[c.variant] << ",split=" << c.policy
+          << ":" << t << "ms;";
       if (t < best) {
         best = t;
         pick = c;
+      }
+      if (ci + 1 == cands.size() && !split_tried) {
+        split_tried = true;
+        cands.push_back({pick.Lmax, pick.threads, 1, pick.variant});
       }
     }
   } catch (...) {
@@ -525,8 +567,9 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
   cudaFree(dout);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  build(*p, pick.Lmax, pick.threads, pick.policy);
-  log << "chosen Lmax=" << pick.Lmax << ",threads=" << pick.threads << ",split=" << pick.policy;
+  build(*p, pick.Lmax, pick.threads, pick.policy, pick.variant);
+  log << "chosen Lmax=" << pick.Lmax << ",threads=" << pick.threads << ",ctas=" << kBatchMinB[pick.variant]
+      << ",split=" << pick.policy;
   p->tune_log = log.str();
   return p.release();
 }
@@ -540,7 +583,8 @@ std::string batch_info(const BatchPlan &p) {
   cudaMemcpy(items.data(), p.d_items, items.size() * sizeof(Item), cudaMemcpyDeviceToHost);
   for (const Item &I : items) counts[I.type]++;
   s << "{\"count\": " << p.count << ", \"elements\": " << p.total << ", \"Lmax\": " << p.Lmax
-    << ", \"threads\": " << p.threads << ", \"split_policy\": " << p.split << ", \"grid\": " << p.grid
+    << ", \"threads\": " << p.threads << ", \"min_ctas_per_sm\": " << kBatchMinB[p.variant]
+    << ", \"split_policy\": " << p.split << ", \"grid\": " << p.grid
     << ", \"direct\": " << counts[0] << ", \"four_step\": " << counts[1] << ", \"bluestein_onchip\": " << counts[2]
     << ", \"bluestein_four_step\": " << counts[3] << ", \"tune\": \"" << p.tune_log << "\"}";
   return s.str();

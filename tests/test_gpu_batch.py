@@ -17,14 +17,19 @@ pytestmark = pytest.mark.gpu
 LENGTHS = [16, 17, 100, 127, 1000, 4096, 4099, 5000, 8192, 12289, 25600, 65536, 65521, 3, 1, 2, 4097, 30030]
 
 
+@pytest.mark.parametrize("ctas", ["1", "3", "4"])
 @pytest.mark.parametrize("lmax", ["2048", "4096", "8192"])
 @pytest.mark.parametrize("dtype", ["complex64", "complex128"])
 @pytest.mark.parametrize("forward", [True, False])
-def test_batch_matches_per_row(rg, cuda, dtype, forward, lmax, monkeypatch):
+def test_batch_matches_per_row(rg, cuda, dtype, forward, lmax, ctas, monkeypatch):
     """Each on-chip capacity (ROCKET_GPU_BATCH_LMAX; 8192 is single precision only, complex128
-    keeps 4096)."""
+    keeps 4096) and register budget (ROCKET_GPU_BATCH_CTAS: the 80- and 64-register instances,
+    single precision only; complex128 keeps the 128-register one)."""
     torch = cuda
+    if dtype == "complex128" and ctas != "1":
+        pytest.skip("one register budget in double precision")
     monkeypatch.setenv("ROCKET_GPU_BATCH_LMAX", lmax)
+    monkeypatch.setenv("ROCKET_GPU_BATCH_CTAS", ctas)
     batch = importlib.import_module("rocket_fft_gb300.batch")
     tdt = getattr(torch, dtype)
     plan = batch.BatchedC2C(LENGTHS, dtype=tdt, forward=forward, fct=0.5, autotune=False)
