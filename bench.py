@@ -954,14 +954,17 @@ def run_sweep(args):
     peak, peak_kind = peaks()
     gen = torch.Generator(device="cuda").manual_seed(17 + rank)
     reps, warm = max(3, min(args.steps, 20)), max(1, min(args.warmup, 3))
+    lo, _, hi = args.exps.partition("-")
+    exps = range(max(10, int(lo)), min(24, int(hi or lo)) + 1)
     with ClockSampler(local) as clk:
-        rows = sweep_rows(torch, rg, gen, peak, reps, warm)
+        rows = sweep_rows(torch, rg, gen, peak, reps, warm, exps)
     if rank == 0:
-        line = {"metric": "fraction of HBM peak, batched complex64 c2c over lengths 2^10..2^24 (lowest)",
+        span = f"2^{exps[0]}..2^{exps[-1]}"
+        line = {"metric": f"fraction of HBM peak, batched complex64 c2c over lengths {span} (lowest)",
                 "value": min(r["c2c_frac"] for r in rows), "unit": "fraction", "n_gpus": world,
                 "steps": reps, "warmup": warm, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (seeded N(0,1))",
-                "config": {"workload": "batched 1-D c2c complex64 and r2c float32, lengths 2^10..2^24, "
+                "config": {"workload": f"batched 1-D c2c complex64 and r2c float32, lengths {span}, "
                                        "about 256 MiB of input per length", "l2": "256 MiB inputs > L2"},
                 "peak": peak, "peak_source": peak_kind, "rows": rows, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
@@ -978,6 +981,8 @@ def main():
                          "256 x 4096; c3: 10,000 uneven complex64 lengths in one launch; c4: "
                          "differentiable rfftn 64 x 1024^2; c5: Neumann Poisson 512^3; sweep: batched "
                          "complex64 c2c / float32 r2c over lengths 2^10..2^24 against the HBM peak")
+    ap.add_argument("--exps", default="10-24",
+                    help="sweep only: log2 lengths LO-HI (default 10-24), e.g. 14-14 for one length")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -492,7 +492,11 @@ BatchPlan *batch_create(const int64_t *lengths, int64_t count, DType dt, bool fo
     const int v = std::atoi(e);
     if ((v == 2048 || v == 4096 || v == 8192) && fits(v)) lmax0 = v;
   }
-  // ROCKET_GPU_BATCH_CTAS (3 or 4, single precision) picks the 80- or 64-register instance
+  // ROCKET_GPU_BATCH_TUNE=0 skips the autotune (the configuration then comes from the two
+  // variables here); ROCKET_GPU_BATCH_CTAS (3 or 4, single precision) picks the 80- or
+  // 64-register instance
+  if (const char *e = std::getenv("ROCKET_GPU_BATCH_TUNE"))
+    if (std::atoi(e) == 0) autotune = false;
   int var0 = 0;
   if (const char *e = std::getenv("ROCKET_GPU_BATCH_CTAS")) {
     const int v = std::atoi(e);

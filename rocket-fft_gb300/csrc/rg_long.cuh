@@ -211,9 +211,14 @@ template <int E1, int E2, int ET> struct LgCfg {
   static constexpr int NT = TT / 16;              // threads: one radix-16 butterfly each
   static constexpr int PA = lg::best_pitch(E1, C, NT, true), PB = lg::best_pitch(E2, D, NT, false);
   static constexpr int SLOTS = C * PA > D * PB ? C * PA : D * PB;
-  // the tile, then two control words (ticket, wait failure): no static shared memory, so the
-  // dynamic size may be raised to the device's opt-in maximum
-  static constexpr size_t SMEM = size_t(SLOTS) * 8 + 16;
+  // radix of phase A's last pass, and its per-tile factors W_n^{col k NS} (k = 1 .. RA-1, one
+  // per column of the tile)
+  static constexpr int RA = fx::radix_of(E1, fx::np_of(E1) - 1);
+  static constexpr int FTAB = (RA - 1) * C;
+  // the tile, the factor table, then two control words (ticket, wait failure): no static
+  // shared memory, so the dynamic size may be raised to the device's opt-in maximum
+  static constexpr size_t CTRL = size_t(SLOTS + FTAB) * 8;
+  static constexpr size_t SMEM = CTRL + 16;
   static_assert(C >= 2 && D >= 2 && C <= 32 && D <= 32, "tile shape");
   static_assert(fx::radix_of(E1, 0) == 16 && fx::radix_of(E2, 0) == 16, "first pass radix 16");
 };
@@ -330,6 +335,21 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
   using Cf = LgCfg<E1, E2, ET>;
   constexpr int N1 = Cf::N1, N2 = Cf::N2, C = Cf::C, NT = Cf::NT, PA = Cf::PA;
   const float2 *tw = reinterpret_cast<const float2 *>(a.twA);
+  const float2 *lo = reinterpret_cast<const float2 *>(a.lo), *hi = reinterpret_cast<const float2 *>(a.hi);
+  // The four-step twiddle of output k1 = j + k NS of column col, W_n^{col k1}, is applied as
+  // W_n^{col j} (one table lookup per butterfly) times W_n^{col k NS} from a per-tile table in
+  // shared memory: looked up per element, the scattered lo-table reads of a warp (one sector per
+  // lane) were most of the kernel's L1 wavefronts. Visible to the last pass after the first
+  // pass's barrier.
+  float2 *ftab = sm + Cf::SLOTS;
+  {
+    constexpr int NS = N1 / Cf::RA;
+    for (int i = int(threadIdx.x); i < Cf::FTAB; i += NT) {
+      const int kk = i / C + 1, cc = i - (kk - 1) * C;
+      const int col = KIND == LG_C2R ? pair_index<N2, C>(part, cc) : part * C + cc;
+      ftab[i] = split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * uint32_t(kk * NS));
+    }
+  }
   if constexpr (KIND != LG_C2R) {
     // first pass: radix 16 straight from global memory; lanes run across the C columns first
     constexpr int R = 16, LR = N1 / R, UNITS = C * LR;
@@ -395,7 +415,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     constexpr int P = fx::np_of(E1) - 1, R = fx::radix_of(E1, P), LR = N1 / R, NS = LR;
     constexpr int UNITS = C * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
-    const float2 *lo = reinterpret_cast<const float2 *>(a.lo), *hi = reinterpret_cast<const float2 *>(a.hi);
+    static_assert(R == Cf::RA, "factor table radix");
     const uint64_t keep = lg::keep_policy();
 #pragma unroll
     for (int it = 0; it < ITER; ++it) {
@@ -405,11 +425,12 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       lg_last_one<E1, PA>(sm, tw, c, j, v);
       const int col = KIND == LG_C2R ? pair_index<N2, C>(part, c) : part * C + c;
       float2 *yc = y + col;
+      const float2 wj = split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * uint32_t(j));
+      lg::st_keep(yc + int64_t(j) * N2, mul<float>(v[0], wj), keep);
 #pragma unroll
-      for (int k = 0; k < R; ++k) {
-        const uint32_t k1 = uint32_t(j + k * NS);
-        const float2 r = mul<float>(v[k], split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * k1));
-        lg::st_keep(yc + int64_t(k1) * N2, r, keep);
+      for (int k = 1; k < R; ++k) {
+        const float2 w = mul<float>(wj, ftab[(k - 1) * C + c]);
+        lg::st_keep(yc + int64_t(j + k * NS) * N2, mul<float>(v[k], w), keep);
       }
     }
   }
@@ -536,7 +557,7 @@ __global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, 1024 / LgCfg<E1, E2, ET
   asm volatile("griddepcontrol.wait;" ::: "memory");
   extern __shared__ __align__(16) unsigned char smraw[];
   float2 *sm = reinterpret_cast<float2 *>(smraw);
-  int &s_t = *reinterpret_cast<int *>(smraw + size_t(Cf::SLOTS) * 8);
+  int &s_t = *reinterpret_cast<int *>(smraw + Cf::CTRL);
   int &s_fail = *(&s_t + 1);
   const int N = a.tiles;
   const int total = 2 * a.ngroups * N;

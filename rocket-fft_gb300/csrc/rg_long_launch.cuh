@@ -28,7 +28,7 @@ void launch_long(LongArgs &a, int64_t tickets, cudaStream_t st) {
   X(7, 7, 10) X(7, 7, 11) X(7, 8, 10) X(7, 8, 11) X(8, 8, 11) X(8, 8, 12) X(8, 9, 11) X(8, 9, 12) \
   X(9, 9, 11) X(9, 9, 12) X(9, 9, 13) X(9, 10, 11) X(9, 10, 12) X(9, 10, 13) X(10, 10, 11)        \
   X(10, 10, 12) X(10, 10, 13) X(10, 11, 12) X(10, 11, 13) X(11, 11, 12) X(11, 11, 13)             \
-  X(11, 11, 14) X(11, 12, 13) X(11, 12, 14)
+  X(11, 11, 14) X(11, 12, 13) X(11, 12, 14) X(7, 7, 12) X(7, 8, 12)
 #define RG_LONG_SHAPES_C2C_ONLY(X) X(12, 12, 13) X(12, 12, 14)
 
 inline bool long_shape_instantiated(int e1, int e2, int et) {
