@@ -15,8 +15,8 @@
 // Y (its HBM writes are D-element segments). Each thread runs one radix butterfly per pass (at
 // most 64 registers, two CTAs of TT / 16 threads per SM). Both phases read their first radix
 // pass straight from global memory into registers and write their last pass straight back; the
-// passes in between run in place in one shared buffer, whose line pitch is chosen at compile
-// time to minimise shared-memory wavefronts over all of the kernel's access patterns.
+// passes in between run in place in one shared buffer, whose line pitch and padding period are
+// chosen at compile time to minimise shared-memory wavefronts over the kernel's access patterns.
 //
 // Y is the only intermediate, and it is kept in L2: transforms go through in groups of G
 // (G * n * 8 bytes of Y per group), and group g uses slot g mod S of a ring of S Y buffers.
@@ -74,17 +74,19 @@ constexpr int kLongEvictOut = 2;
 
 namespace lg {
 
-// shared index of position pos of a line: one pad slot per 32 positions
-__host__ __device__ constexpr int sp(int pos) { return pos + (pos >> 5); }
+// shared index of position pos of a line: one pad slot per 2^PS positions (PS = 3, 4 or 5,
+// chosen per phase together with the line pitch)
+__host__ __device__ constexpr int spad(int pos, int ps) { return pos + (pos >> ps); }
 
-// sp(base + k * STEP) as the base's index plus a compile-time offset, for the runs the passes
-// use: STEP a multiple of 32 (any base), STEP 16 with base % 32 < 16, STEP 1 with
-// base % 32 + k < 32 (checked for every access of every instantiated length); else sp().
-template <int STEP> __device__ __forceinline__ int sp_k(int base, int k) {
-  if constexpr (STEP % 32 == 0) return base + (base >> 5) + k * (STEP + STEP / 32);
-  else if constexpr (STEP == 16) return base + (base >> 5) + 16 * k + (k >> 1);
-  else if constexpr (STEP == 1) return base + (base >> 5) + k;
-  else return sp(base + k * STEP);
+// spad(base + k * STEP, PS) as the base's index plus a compile-time offset, for the runs the
+// passes use: STEP a multiple of 2^PS (any base); STEP 16 with PS 5 and base % 32 < 16; STEP 1
+// with base a multiple of 16 (the first-pass writes, base = 16 j, k < 16); else spad().
+template <int STEP, int PS> __device__ __forceinline__ int sp_k(int base, int k) {
+  if constexpr (STEP % (1 << PS) == 0) return base + (base >> PS) + k * (STEP + (STEP >> PS));
+  else if constexpr (PS == 5 && STEP == 16) return base + (base >> 5) + 16 * k + (k >> 1);
+  else if constexpr (STEP == 1 && PS == 5) return base + (base >> 5) + k;
+  else if constexpr (STEP == 1) return base + (base >> PS) + k + (k >> PS);
+  else return spad(base + k * STEP, PS);
 }
 
 __device__ __forceinline__ uint64_t globaltimer() {
@@ -137,21 +139,27 @@ __device__ __forceinline__ void discard_l2(const void *p) {
 
 }  // namespace lg
 
-// Shared-memory wavefronts (8-byte slots, 16 per 128-byte wavefront) of the lanes of warp w over
-// one tile phase whose M lines of length 2^E sit `pitch` slots apart: the first pass's writes,
-// every middle pass's reads and writes and the last pass's reads, each with its lane-to-(line,
-// position) mapping. `across`: the first and last passes run lanes across the lines first (phase
-// A: the columns; phase B: only its last pass).
+// Shared-memory wavefronts of the lanes of the first warps over one tile phase whose M lines of
+// length 2^E sit `pitch` slots apart (padding period 2^ps): the first pass's writes, every middle
+// pass's reads and writes and the last pass's reads, each with its lane-to-(line, position)
+// mapping. `a_side`: the first and last passes run lanes across the lines first (phase A: the
+// columns; phase B: only its last pass). A warp's 8-byte accesses are served one half-warp at a
+// time, 16 slots (128 bytes) per wavefront; this count matched the bank conflicts ncu measured
+// on GB300 (2^14 points: 6.3 M modelled, 6.4 M measured excess store wavefronts).
 namespace lg {
 constexpr int wave(const int (&slot)[32]) {
-  int cnt[16] = {}, worst = 0;
-  for (int l = 0; l < 32; ++l) {
-    const int b = slot[l] & 15;
-    if (++cnt[b] > worst) worst = cnt[b];
+  int total = 0;
+  for (int h = 0; h < 2; ++h) {
+    int cnt[16] = {}, worst = 0;
+    for (int l = 16 * h; l < 16 * h + 16; ++l) {
+      const int b = slot[l] & 15;
+      if (++cnt[b] > worst) worst = cnt[b];
+    }
+    total += worst;
   }
-  return worst;
+  return total;
 }
-constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side) {
+constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps) {
   const int L = 1 << E, NP = fx::np_of(E);
   int total = 0;
   for (int w = 0; w < NT / 32 && w < 4; ++w) {
@@ -161,7 +169,7 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side) {
       for (int l = 0; l < 32; ++l) {
         const int u = 32 * w + l;
         const int line = a_side ? u % M : u / (L / 16), j = a_side ? u / M : u % (L / 16);
-        slot[l] = line * pitch + sp(16 * j + k);
+        slot[l] = line * pitch + spad(16 * j + k, ps);
       }
       total += wave(slot);
     }
@@ -173,14 +181,14 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side) {
             const int u = 32 * w + l + it * NT;
             const bool last = p == NP - 1;
             const int line = last ? u % M : u / LR, j = last ? u / M : u % LR;
-            slot[l] = line * pitch + sp(j + k * LR);
+            slot[l] = line * pitch + spad(j + k * LR, ps);
           }
           total += wave(slot);
           if (p < NP - 1) {
             for (int l = 0; l < 32; ++l) {  // writes of a middle pass
               const int u = 32 * w + l + it * NT;
               const int line = u / LR, j = u % LR, m = j & (NS - 1);
-              slot[l] = line * pitch + sp((j - m) * R + m + k * NS);
+              slot[l] = line * pitch + spad((j - m) * R + m + k * NS, ps);
             }
             total += wave(slot);
           }
@@ -189,18 +197,27 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side) {
   }
   return total;
 }
-// The pitch (>= the padded line length, within 16 slots of it) with the fewest wavefronts.
-constexpr int best_pitch(int E, int M, int NT, bool a_side) {
-  const int base = sp((1 << E) - 1) + 1;
-  int best = base, cost = 1 << 30;
+// For padding period 2^ps: the pitch (>= the padded line length, within 16 slots of it) with
+// the fewest wavefronts, as cost * 2^16 + pitch.
+constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps) {
+  const int base = spad((1 << E) - 1, ps) + 1;
+  int best = base, cost = 1 << 14;
   for (int p = base; p < base + 16; ++p) {
-    const int c = phase_waves(E, M, NT, p, a_side);
+    const int c = phase_waves(E, M, NT, p, a_side, ps);
     if (c < cost) {
       cost = c;
       best = p;
     }
   }
-  return best;
+  return (cost << 16) + best;
+}
+// Of three such choices (periods 32, 16, 8), the one with the fewest wavefronts, as
+// log2 period * 2^16 + pitch; ties keep the longer period (less padding).
+constexpr int pick_layout(int c5, int c4, int c3) {
+  const int k5 = c5 >> 16, k4 = c4 >> 16, k3 = c3 >> 16;
+  if (k5 <= k4 && k5 <= k3) return (5 << 16) + (c5 & 0xffff);
+  if (k4 <= k3) return (4 << 16) + (c4 & 0xffff);
+  return (3 << 16) + (c3 & 0xffff);
 }
 }  // namespace lg
 
@@ -209,7 +226,15 @@ template <int E1, int E2, int ET> struct LgCfg {
   static constexpr int N1 = 1 << E1, N2 = 1 << E2, TT = 1 << ET;
   static constexpr int C = TT / N1, D = TT / N2;  // columns per A tile, rows per B tile
   static constexpr int NT = TT / 16;              // threads: one radix-16 butterfly each
-  static constexpr int PA = lg::best_pitch(E1, C, NT, true), PB = lg::best_pitch(E2, D, NT, false);
+  // shared layout of each phase: padding period and line pitch (each candidate period searched
+  // in a constant of its own, within the compiler's constant-evaluation budget)
+  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5), A4 = lg::best_pitch(E1, C, NT, true, 4);
+  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3);
+  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5), B4 = lg::best_pitch(E2, D, NT, false, 4);
+  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3);
+  static constexpr int LA = lg::pick_layout(A5, A4, A3), LB = lg::pick_layout(B5, B4, B3);
+  static constexpr int PA = LA & 0xffff, PB = LB & 0xffff;  // line pitches (slots)
+  static constexpr int SA = LA >> 16, SB = LB >> 16;        // padding periods (log2)
   static constexpr int SLOTS = C * PA > D * PB ? C * PA : D * PB;
   // radix of phase A's last pass, and its per-tile factors W_n^{col k NS} (k = 1 .. RA-1, one
   // per column of the tile)
@@ -226,7 +251,7 @@ template <int E1, int E2, int ET> struct LgCfg {
 // ---- passes over lines of length 2^E held in shared memory (line l at sm + l * PITCH) ----
 
 // Middle pass P, in place: all butterflies read (and transform) before a barrier, then write.
-template <int E, int P, int M, int NT, int PITCH>
+template <int E, int P, int M, int NT, int PITCH, int PS>
 __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__ tw) {
   constexpr int L = 1 << E, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P), TWO = fx::tw_of(E, P);
   constexpr int UNITS = M * LR, ITER = (UNITS + NT - 1) / NT;
@@ -238,7 +263,7 @@ __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__
     const int line = u / LR, j = u % LR;
     const float2 *s = sm + line * PITCH;
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[it][k] = s[lg::sp_k<LR>(j, k)];
+    for (int k = 0; k < R; ++k) v[it][k] = s[lg::sp_k<LR, PS>(j, k)];
     if constexpr (NS > 1) {
       const float2 *t = tw + TWO + (j & (NS - 1));
 #pragma unroll
@@ -254,22 +279,22 @@ __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__
     const int m = j & (NS - 1), base = (j - m) * R + m;
     float2 *s = sm + line * PITCH;
 #pragma unroll
-    for (int k = 0; k < R; ++k) s[lg::sp_k<NS>(base, k)] = v[it][k];
+    for (int k = 0; k < R; ++k) s[lg::sp_k<NS, PS>(base, k)] = v[it][k];
   }
   __syncthreads();
 }
 
-template <int E, int M, int NT, int PITCH, int P, int PEND>
+template <int E, int M, int NT, int PITCH, int PS, int P, int PEND>
 __device__ __forceinline__ void lg_middles(float2 *sm, const float2 *__restrict__ tw) {
   if constexpr (P < PEND) {
-    lg_middle<E, P, M, NT, PITCH>(sm, tw);
-    lg_middles<E, M, NT, PITCH, P + 1, PEND>(sm, tw);
+    lg_middle<E, P, M, NT, PITCH, PS>(sm, tw);
+    lg_middles<E, M, NT, PITCH, PS, P + 1, PEND>(sm, tw);
   }
 }
 
 // Last-pass butterfly j of line l: inputs from shared memory, twiddled, transformed; output k
 // lands at position j + k * NS of the transform.
-template <int E, int PITCH>
+template <int E, int PITCH, int PS>
 __device__ __forceinline__ void lg_last_one(const float2 *sm, const float2 *__restrict__ tw, int l, int j,
                                             float2 (&a)[fx::radix_of(E, fx::np_of(E) - 1)]) {
   constexpr int L = 1 << E, P = fx::np_of(E) - 1, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P);
@@ -277,7 +302,7 @@ __device__ __forceinline__ void lg_last_one(const float2 *sm, const float2 *__re
   static_assert(NS == LR, "last pass");
   const float2 *s0 = sm + l * PITCH;
 #pragma unroll
-  for (int k = 0; k < R; ++k) a[k] = s0[lg::sp_k<LR>(j, k)];
+  for (int k = 0; k < R; ++k) a[k] = s0[lg::sp_k<LR, PS>(j, k)];
   if constexpr (NS > 1) {
     const float2 *t = tw + TWO + j;
 #pragma unroll
@@ -333,7 +358,7 @@ template <int KIND, int E1, int E2, int ET>
 __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const float2 *__restrict__ x,
                                            float2 *__restrict__ y, int part) {
   using Cf = LgCfg<E1, E2, ET>;
-  constexpr int N1 = Cf::N1, N2 = Cf::N2, C = Cf::C, NT = Cf::NT, PA = Cf::PA;
+  constexpr int N1 = Cf::N1, N2 = Cf::N2, C = Cf::C, NT = Cf::NT, PA = Cf::PA, SA = Cf::SA;
   const float2 *tw = reinterpret_cast<const float2 *>(a.twA);
   const float2 *lo = reinterpret_cast<const float2 *>(a.lo), *hi = reinterpret_cast<const float2 *>(a.hi);
   // The four-step twiddle of output k1 = j + k NS of column col, W_n^{col k1}, is applied as
@@ -369,9 +394,9 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     dft<float, R>(v);
     float2 *l0 = sm + c * PA;
 #pragma unroll
-    for (int k = 0; k < R; ++k) l0[lg::sp_k<1>(j * R, k)] = v[k];
+    for (int k = 0; k < R; ++k) l0[lg::sp_k<1, SA>(j * R, k)] = v[k];
     __syncthreads();
-    lg_middles<E1, C, NT, PA, 1, fx::np_of(E1) - 1>(sm, tw);
+    lg_middles<E1, C, NT, PA, SA, 1, fx::np_of(E1) - 1>(sm, tw);
   } else {
     // c2r: merge the half spectrum X (m + 1 elements, m = n1 n2) of columns j2 and n2 - j2
     // into conj(Z) on chip, then every pass but the last in shared memory
@@ -394,8 +419,8 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       const float2 A = add<float>(xa, cj<float>(xb)), B = sub<float>(xa, cj<float>(xb));
       const float2 w = split_twiddle<float>(lo2, hi2, a.shift2, uint32_t(ja));
       const float2 uu = mposi<float>(mulc<float>(B, w));
-      sm[la * PA + lg::sp(pa)] = cj<float>(add<float>(A, uu));
-      if (two) sm[lb * PA + lg::sp(pb)] = sub<float>(A, uu);
+      sm[la * PA + lg::spad(pa, SA)] = cj<float>(add<float>(A, uu));
+      if (two) sm[lb * PA + lg::spad(pb, SA)] = sub<float>(A, uu);
     };
     const int t = part;
     for (int u = int(threadIdx.x); u < H * N1; u += NT) {
@@ -407,7 +432,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     }
     if (t == 0 && threadIdx.x == 0) merge(0, N1 / 2, 0, N1 / 2, M / 2, false);
     __syncthreads();
-    lg_middles<E1, C, NT, PA, 0, fx::np_of(E1) - 1>(sm, tw);
+    lg_middles<E1, C, NT, PA, SA, 0, fx::np_of(E1) - 1>(sm, tw);
   }
   // last pass: outputs k1 = j + k * NS, times W_n^{j2 k1}, to Y[k1][j2]; lanes across the C
   // columns first (L2-resident stores, kept there with an evict-last policy)
@@ -422,7 +447,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       const int u = int(threadIdx.x) + it * NT;
       const int c = u % C, j = u / C;
       float2 v[R];
-      lg_last_one<E1, PA>(sm, tw, c, j, v);
+      lg_last_one<E1, PA, SA>(sm, tw, c, j, v);
       const int col = KIND == LG_C2R ? pair_index<N2, C>(part, c) : part * C + c;
       float2 *yc = y + col;
       const float2 wj = split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * uint32_t(j));
@@ -442,7 +467,7 @@ template <int KIND, int E1, int E2, int ET>
 __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const float2 *__restrict__ yg,
                                            float2 *__restrict__ X, int part) {
   using Cf = LgCfg<E1, E2, ET>;
-  constexpr int N1 = Cf::N1, N2 = Cf::N2, D = Cf::D, NT = Cf::NT, PB = Cf::PB;
+  constexpr int N1 = Cf::N1, N2 = Cf::N2, D = Cf::D, NT = Cf::NT, PB = Cf::PB, SB = Cf::SB;
   const float2 *tw = reinterpret_cast<const float2 *>(a.twB);
   // row of Y held by line r
   auto yrow = [&](int r) -> const float2 * {
@@ -462,7 +487,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     dft<float, R>(v);
     float2 *l = sm + r * PB;
 #pragma unroll
-    for (int k = 0; k < R; ++k) l[lg::sp_k<1>(j * R, k)] = v[k];
+    for (int k = 0; k < R; ++k) l[lg::sp_k<1, SB>(j * R, k)] = v[k];
   }
   __syncthreads();
   if (a.flags & kLongDiscard) {
@@ -475,7 +500,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
   const float sgn = a.conj_out ? -fct : fct;
   const uint64_t pol = input_policy((a.flags & kLongEvictOut) != 0);
   if constexpr (KIND != LG_R2C) {
-    lg_middles<E2, D, NT, PB, 1, fx::np_of(E2) - 1>(sm, tw);
+    lg_middles<E2, D, NT, PB, SB, 1, fx::np_of(E2) - 1>(sm, tw);
     // last pass: outputs k2 = j + k * NS of row r to X[r + k2 n1]; lanes across the D rows first
     constexpr int P = fx::np_of(E2) - 1, R = fx::radix_of(E2, P), LR = N2 / R, NS = LR;
     constexpr int UNITS = D * LR, ITER = UNITS / NT;
@@ -486,7 +511,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
       const int u = int(threadIdx.x) + it * NT;
       const int r = u % D, j = u / D;
       float2 v[R];
-      lg_last_one<E2, PB>(sm, tw, r, j, v);
+      lg_last_one<E2, PB, SB>(sm, tw, r, j, v);
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const int64_t k2 = j + k * NS;
@@ -495,7 +520,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     }
   } else {
     // r2c: every pass on chip, then the split of each row pair into X_k and X_{m-k}
-    lg_middles<E2, D, NT, PB, 1, fx::np_of(E2)>(sm, tw);
+    lg_middles<E2, D, NT, PB, SB, 1, fx::np_of(E2)>(sm, tw);
     constexpr int64_t M = int64_t(N1) * N2;
     constexpr int H = D / 2;
     const float2 *lo2 = reinterpret_cast<const float2 *>(a.lo2), *hi2 = reinterpret_cast<const float2 *>(a.hi2);
@@ -506,7 +531,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
                    : "memory");
     };
     auto split = [&](int la, int pa, int lb, int pb, int64_t ka, bool two) {
-      const float2 za = sm[la * PB + lg::sp(pa)], zc = cj<float>(sm[lb * PB + lg::sp(pb)]);
+      const float2 za = sm[la * PB + lg::spad(pa, SB)], zc = cj<float>(sm[lb * PB + lg::spad(pb, SB)]);
       const float2 Ev = scl<float>(add<float>(za, zc), 0.5f);
       const float2 O = mnegi<float>(scl<float>(sub<float>(za, zc), 0.5f));
       const float2 t = mul<float>(split_twiddle<float>(lo2, hi2, a.shift2, uint32_t(ka)), O);
