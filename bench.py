@@ -46,6 +46,10 @@ WORKLOAD = "3-D r2c + c2r round trip, float32 256x256x256, axes [0,1,2], fct 1 a
 # dirty in L2 when the launch ends. Only the default line uses it (the other workloads' kernels
 # of the same name run other lengths).
 NCU_TRAFFIC = {"axis_c2c_f32": 67_653_632 + 7_301_376}
+# The same for the batch kernel on the 10,000-length batch (seed 0, the autotuned configuration
+# pinned: capacity 4096, three CTAs per SM): 20.84 GB read + 16.11 GB written per launch, 9.0 x
+# the 4.12 GB of algorithmic bytes (the four-step and Bluestein workspaces).
+NCU_TRAFFIC_C3 = 20_839_577_344 + 16_113_419_520
 
 
 def load_package():
@@ -321,7 +325,8 @@ def c3_form(torch, rg, steps):
                         "[16, 65536]), one persistent launch from a CUDA graph", "value": len(rows) / (ms / 1e3),
             "unit": "transforms/s", "ms_per_batch": ms, "per_launch_ms": per_ms, "vs_per_launch": per_ms / ms,
             "per_launch_note": "10,000 host-issued c2c calls, device time between events: includes issue cost",
-            "planning_s_incl_autotune": plan_s}
+            "planning_s_incl_autotune": plan_s, "plan": plan.info(),
+            "traffic_per_batch": NCU_TRAFFIC_C3, "traffic_vs_algorithmic": NCU_TRAFFIC_C3 / (2 * plan.total * 8)}
 
 
 def run_c1(args):
@@ -642,7 +647,9 @@ def run_c3(args):
                       "l2": f"{bytes_step / 1e9:.1f} GB per step > L2", "plan": plan.info(),
                       "planning_s_incl_autotune": plan_s})
     line.update({"roofline": {"bound": "hbm", "kernel": "batch_kernel<float>", "achieved": achieved, "peak": peak,
-                              "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                              "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                              "traffic": NCU_TRAFFIC_C3 if rank == 0 else None,
+                              "traffic_vs_algorithmic": NCU_TRAFFIC_C3 / bytes_step if rank == 0 else None,
                               "launch_ms": ms / args.steps, "bytes_per_launch": bytes_step, "share": 1.0},
                  "per_transform_launches": {"gpu_ms": per_launch_ms, "wall_ms": per_launch_wall * 1e3,
                                             "transforms_per_s_gpu": len(rows) / (per_launch_ms / 1e3),
