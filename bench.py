@@ -47,9 +47,9 @@ WORKLOAD = "3-D r2c + c2r round trip, float32 256x256x256, axes [0,1,2], fct 1 a
 # of the same name run other lengths).
 NCU_TRAFFIC = {"axis_c2c_f32": 67_653_632 + 7_301_376}
 # The same for the batch kernel on the 10,000-length batch (seed 0, the autotuned configuration
-# pinned: capacity 4096, three CTAs per SM): 20.84 GB read + 16.11 GB written per launch, 9.0 x
+# pinned: capacity 4096, three CTAs per SM): 15.07 GB read + 8.82 GB written per launch, 5.8 x
 # the 4.12 GB of algorithmic bytes (the four-step and Bluestein workspaces).
-NCU_TRAFFIC_C3 = 20_839_577_344 + 16_113_419_520
+NCU_TRAFFIC_C3 = 15_067_335_936 + 8_818_280_960
 
 
 def load_package():

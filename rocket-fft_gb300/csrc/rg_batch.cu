@@ -126,9 +126,11 @@ template <typename T> struct K {
   // four-step twiddle W_N^{(col0 + r) * i}; optional conj/fct; optional *bk (y = conj(F*bk), bk
   // indexed like the output: bk[r*rstride + i*estride]).
   // colwalk: consecutive threads take consecutive rows (rows adjacent in memory, rstride 1).
+  // Elements at offsets r*rstride + i*estride >= lim are not stored.
   __device__ void store(const cx<T> *res, cx<T> *base, int rows, int len, int64_t rstride, int64_t estride,
                         bool conj_out, T scale, const cx<T> *lo = nullptr, const cx<T> *hi = nullptr, int shift = 0,
-                        int col0 = 0, const cx<T> *bk = nullptr, int nvalid = 1 << 30, bool colwalk = false) {
+                        int col0 = 0, const cx<T> *bk = nullptr, int nvalid = 1 << 30, bool colwalk = false,
+                        int64_t lim = INT64_MAX) {
     const int total = rows * len;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
       int r, i;
@@ -139,7 +141,7 @@ template <typename T> struct K {
         r = e / len;
         i = e - r * len;
       }
-      if (i >= nvalid) continue;
+      if (i >= nvalid || r * rstride + i * estride >= lim) continue;
       cx<T> v = res[sidx(r, i, pitch, a.ps)];
       if (lo) v = mul<T>(v, split_twiddle<T>(lo, hi, shift, uint32_t(col0 + r) * uint32_t(i)));
       if (bk) v = cj<T>(mul<T>(v, bk[r * rstride + i * estride]));
@@ -147,6 +149,92 @@ template <typename T> struct K {
       base[r * rstride + i * estride] = v;
     }
     __syncthreads();
+  }
+
+  // Columns c0 .. c0+rows-1 of src viewed as n1 x n2 (column j2 = c0 + r: elements j1 at
+  // src[j1 * n2 + j2]) into shared buffer s0 as rows of length n1; the Bluestein chirp and
+  // padding use the global index j = j1 * n2 + j2. Columns fastest: consecutive threads read
+  // consecutive j2 of one j1 (coalesced); kBatch loads per thread in flight before the shared
+  // stores.
+  __device__ void load_cols(const cx<T> *src, int n1, int n2, int c0, int rows, bool conj_in, const cx<T> *bk_in,
+                            int nvalid_in) {
+    const int total = rows * n1;
+    const int nth = blockDim.x;
+    for (int e0 = threadIdx.x; e0 < total; e0 += nth * kBatch) {
+      cx<T> v[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * nth;
+        v[u] = mk<T>(T(0), T(0));
+        if (e < total) {
+          const int j1 = e / rows, r = e - j1 * rows;
+          const int j = j1 * n2 + c0 + r;
+          if (j < nvalid_in) {
+            v[u] = src[j];
+            if (conj_in) v[u].y = -v[u].y;
+            if (bk_in) v[u] = mulc<T>(v[u], bk_in[j]);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * nth;
+        if (e < total) {
+          const int j1 = e / rows, r = e - j1 * rows;
+          s0[sidx(r, j1, pitch, a.ps)] = v[u];
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // Bluestein convolution of length m = m1 * m2 in three passes over one workspace w (m
+  // elements), y = conj(F(W) bk) * scale with W = conj(F(x conj(bk)) bkf) -- the same product
+  // as two full four-step FFTs, with the inverse's row FFTs run in the same residency as the
+  // forward's:
+  //   columns j2:  DFT_m1 over j1 of x[j1 m2 + j2] conj(bk) (zero from n on), times
+  //                W_m^{j2 k1}, to w[k1 m2 + j2]
+  //   rows k1:     DFT_m2 over j2 gives F(a)[k1 + m1 k2] along the row; times bkf there,
+  //                conjugated: W[k1 + m1 k2]; DFT_m2 over k2, times W_m^{q k1}, back to
+  //                w[k1 m2 + q]
+  //   columns q:   DFT_m1 over k1 gives F(W)[m2 p + q]; outputs j = m2 p + q < n to y, times bk,
+  //                conjugated and scaled
+  // (F(W)[m2 p + q] = sum_k1 W_m1^{p k1} W_m^{q k1} sum_k2 W[k1 + m1 k2] W_m2^{q k2}.)
+  __device__ void blue_conv(const cx<T> *x, cx<T> *y, cx<T> *w, int n, int m1, int m2, const FFTCore &c1,
+                            const FFTCore &c2, const cx<T> *lo, const cx<T> *hi, int shift, const cx<T> *bk,
+                            const cx<T> *bkf, bool conj_in, bool conj_out, T scale) {
+    const int tbA = rows_for(m1);
+    for (int c0 = 0; c0 < m2; c0 += tbA) {
+      const int rows = min(tbA, m2 - c0);
+      load_cols(x, m1, m2, c0, rows, conj_in, bk, n);
+      cx<T> *res = fft(rows, c1);
+      store(res, w + c0, rows, m1, 1, m2, false, T(1), lo, hi, shift, c0, nullptr, 1 << 30, true);
+    }
+    __syncthreads();
+    const int tbB = rows_for(m2);
+    for (int k0 = 0; k0 < m1; k0 += tbB) {
+      const int rows = min(tbB, m1 - k0);
+      load(w + int64_t(k0) * m2, rows, m2, m2, 1, false);
+      cx<T> *res = fft(rows, c2);
+      // spectrum product into s0 (the next FFT's input); rows fastest, so that the bkf reads
+      // (index k1 + m1 k2) are consecutive
+      for (int e = threadIdx.x; e < rows * m2; e += blockDim.x) {
+        const int i = e / rows, r = e - i * rows;
+        const int si = sidx(r, i, pitch, a.ps);
+        s0[si] = cj<T>(mul<T>(res[si], bkf[(k0 + r) + int64_t(m1) * i]));
+      }
+      __syncthreads();
+      res = fft(rows, c2);
+      store(res, w + int64_t(k0) * m2, rows, m2, m2, 1, false, T(1), lo, hi, shift, k0);
+    }
+    __syncthreads();
+    rows_for(m1);
+    for (int c0 = 0; c0 < m2; c0 += tbA) {
+      const int rows = min(tbA, m2 - c0);
+      load_cols(w, m1, m2, c0, rows, false, nullptr, 1 << 30);
+      cx<T> *res = fft(rows, c1);
+      store(res, y + c0, rows, m1, 1, m2, conj_out, scale, nullptr, nullptr, 0, 0, bk + c0, 1 << 30, true, n - c0);
+    }
   }
 
   // dst = DFT_n(src) for n = n1 * n2 through `tmp` (column pass, then row pass); with bk_out the
@@ -160,38 +248,7 @@ template <typename T> struct K {
     const int tbA = rows_for(n1);
     for (int c0 = 0; c0 < n2; c0 += tbA) {
       const int rows = min(tbA, n2 - c0);
-      // column j2 = c0 + r: elements j1 at src[j1 * n2 + j2]; Bluestein chirp/padding uses the
-      // global index j = j1 * n2 + j2
-      const int total = rows * n1;
-      const int nth = blockDim.x;
-      for (int e0 = threadIdx.x; e0 < total; e0 += nth * kBatch) {
-        // columns fastest: consecutive threads read consecutive j2 of one j1 (coalesced); kBatch
-        // loads per thread in flight before the shared stores
-        cx<T> v[kBatch];
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-          const int e = e0 + u * nth;
-          v[u] = mk<T>(T(0), T(0));
-          if (e < total) {
-            const int j1 = e / rows, r = e - j1 * rows;
-            const int j = j1 * n2 + c0 + r;
-            if (j < nvalid_in) {
-              v[u] = src[j];
-              if (conj_in) v[u].y = -v[u].y;
-              if (bk_in) v[u] = mulc<T>(v[u], bk_in[j]);
-            }
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-          const int e = e0 + u * nth;
-          if (e < total) {
-            const int j1 = e / rows, r = e - j1 * rows;
-            s0[sidx(r, j1, pitch, a.ps)] = v[u];
-          }
-        }
-      }
-      __syncthreads();
+      load_cols(src, n1, n2, c0, rows, conj_in, bk_in, nvalid_in);
       cx<T> *res = fft(rows, c1);
       store(res, tmp + c0, rows, n1, 1, n2, false, T(1), lo, hi, shift, c0, nullptr, 1 << 30, true);
     }
@@ -258,19 +315,9 @@ __global__ void __launch_bounds__(kBatchNT[V], kBatchMinB[V]) batch_kernel(const
       }
       res = k.fft(1, a.cores[I.core0]);
       k.store(res, y, 1, I.n, 0, 1, k.bwd, k.fct, nullptr, nullptr, 0, 0, bk, I.n);
-    } else {  // IT_BLUE_FOUR: workspace w holds 2m elements (A, B)
-      cx<T> *A = w, *B = w + I.m;
-      // A = conj(FFT(x conj(bk)) * bkf): the spectrum product fused into the first FFT's store
-      k.four_step(x, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, k.bwd, false, T(1), bk, I.n,
-                  bkf);
-      __syncthreads();
-      k.four_step(A, A, B, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, false, false, T(1));
-      __syncthreads();
-#pragma unroll 4
-      for (int i = threadIdx.x; i < I.n; i += blockDim.x) {
-        cx<T> v = cj<T>(mul<T>(A[i], bk[i]));
-        y[i] = mk<T>(v.x * k.fct, (k.bwd ? -v.y : v.y) * k.fct);
-      }
+    } else {  // IT_BLUE_FOUR: workspace w holds m elements
+      k.blue_conv(x, y, w, I.n, I.n1, I.n2, a.cores[I.core0], a.cores[I.core1], lo, hi, I.tw_shift, bk, bkf, k.bwd,
+                  k.bwd, k.fct);
       __syncthreads();
     }
   }
@@ -406,7 +453,7 @@ void build(BatchPlan &p, int Lmax, int threads, int policy, int variant) {
         I.tw_lo = t.lo;
         I.tw_hi = t.hi;
         I.tw_shift = t.shift;
-        wsoff += 2 * int64_t(I.m);
+        wsoff += int64_t(I.m);
       }
     }
     off += n;
