@@ -237,18 +237,14 @@ template <typename T> struct K {
     }
   }
 
-  // dst = DFT_n(src) for n = n1 * n2 through `tmp` (column pass, then row pass); with bk_out the
-  // row pass stores conj(DFT * bk_out) (the Bluestein spectrum product, fused into the store)
+  // dst = DFT_n(src) for n = n1 * n2 through `tmp` (column pass, then row pass)
   __device__ void four_step(const cx<T> *src, cx<T> *dst, cx<T> *tmp, int n1, int n2, const FFTCore &c1,
                             const FFTCore &c2, const cx<T> *lo, const cx<T> *hi, int shift, bool conj_in,
-                            bool conj_out, T scale, const cx<T> *bk_in = nullptr, int nvalid_in = 1 << 30,
-                            const cx<T> *bk_out = nullptr) {
-    const int64_t n = int64_t(n1) * n2;
-    (void)n;
+                            bool conj_out, T scale) {
     const int tbA = rows_for(n1);
     for (int c0 = 0; c0 < n2; c0 += tbA) {
       const int rows = min(tbA, n2 - c0);
-      load_cols(src, n1, n2, c0, rows, conj_in, bk_in, nvalid_in);
+      load_cols(src, n1, n2, c0, rows, conj_in, nullptr, 1 << 30);
       cx<T> *res = fft(rows, c1);
       store(res, tmp + c0, rows, n1, 1, n2, false, T(1), lo, hi, shift, c0, nullptr, 1 << 30, true);
     }
@@ -258,8 +254,7 @@ template <typename T> struct K {
       const int rows = min(tbB, n1 - k0);
       load(tmp + int64_t(k0) * n2, rows, n2, n2, 1, false);
       cx<T> *res = fft(rows, c2);
-      store(res, dst + k0, rows, n2, 1, n1, conj_out, scale, nullptr, nullptr, 0, 0, bk_out ? bk_out + k0 : nullptr,
-            1 << 30, true);
+      store(res, dst + k0, rows, n2, 1, n1, conj_out, scale, nullptr, nullptr, 0, 0, nullptr, 1 << 30, true);
     }
   }
 };

@@ -224,6 +224,62 @@ __global__ void __launch_bounds__(256) fx_residual_kernel(const long long *U, co
   }
 }
 
+// The same residual as a row sweep, for even n2 with 16-byte aligned rows: each thread takes
+// two adjacent elements of a row (16-byte loads of U and F, 8-byte of Frem, an 8-byte store of
+// r), the CTAs sweep the rows together (sweep_row: a stencil's neighbours one plane away are
+// recent L2 lines), and each CTA adds its sum to *sum once. The one-element form issued a CTA
+// and a double atomic per 256 elements (524,288 atomics on one address for 512^3).
+__device__ __forceinline__ float fx_res_one(unsigned long long c, unsigned long long nb, long long f, float frem,
+                                            int e) {
+  // modulo-2^64 arithmetic: the intermediate sums may wrap, the result (f minus a second
+  // difference, small) is exact
+  const long long R = (long long)((unsigned long long)f - (nb - 6ull * c));
+  return ldexpf(ll_to_float(R), -e) + frem;
+}
+
+__global__ void __launch_bounds__(256) fx_residual_rows_kernel(const long long *U, const long long *F,
+                                                               const float *Frem, float *r32, Grid g, int e, int k,
+                                                               double *sum) {
+  const int64_t rows = g.n0 * g.n1, s0 = g.n1 * g.n2, s1 = g.n2;
+  float acc = 0.f;
+  for (int64_t t = 0; t * gridDim.x < rows; ++t) {
+    const int64_t row = sweep_row(t, 0, 1);
+    if (row >= rows) break;
+    const int64_t k0 = row / g.n1, k1 = row - k0 * g.n1;
+    const int64_t base = row * g.n2;
+    const int64_t o0m = k0 > 0 ? -s0 : 0, o0p = k0 + 1 < g.n0 ? s0 : 0;
+    const int64_t o1m = k1 > 0 ? -s1 : 0, o1p = k1 + 1 < g.n1 ? s1 : 0;
+    for (int64_t k2 = 2 * int64_t(threadIdx.x); k2 < g.n2; k2 += 2 * int64_t(blockDim.x)) {
+      const int64_t i = base + k2;
+      const longlong2 c = *reinterpret_cast<const longlong2 *>(U + i);
+      const longlong2 m0 = *reinterpret_cast<const longlong2 *>(U + i + o0m);
+      const longlong2 p0 = *reinterpret_cast<const longlong2 *>(U + i + o0p);
+      const longlong2 m1 = *reinterpret_cast<const longlong2 *>(U + i + o1m);
+      const longlong2 p1 = *reinterpret_cast<const longlong2 *>(U + i + o1p);
+      const long long left = k2 > 0 ? U[i - 1] : c.x;
+      const long long right = k2 + 2 < g.n2 ? U[i + 2] : c.y;
+      const longlong2 f = *reinterpret_cast<const longlong2 *>(F + i);
+      const float2 fr = Frem ? *reinterpret_cast<const float2 *>(Frem + i) : make_float2(0.f, 0.f);
+      typedef unsigned long long u64;
+      const u64 nx = ((u64)m0.x + (u64)p0.x) + ((u64)m1.x + (u64)p1.x) + ((u64)left + (u64)c.y);
+      const u64 ny = ((u64)m0.y + (u64)p0.y) + ((u64)m1.y + (u64)p1.y) + ((u64)c.x + (u64)right);
+      const float rx = fx_res_one((u64)c.x, nx, f.x, fr.x, e), ry = fx_res_one((u64)c.y, ny, f.y, fr.y, e);
+      if (r32) *reinterpret_cast<float2 *>(r32 + i) = make_float2(rx, ry);
+      const float sx = ldexpf(rx, -k), sy = ldexpf(ry, -k);
+      acc = fmaf(sx, sx, fmaf(sy, sy, acc));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ float red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += double(red[w]);
+    atomicAdd(sum, std::ldexp(t, 2 * k));
+  }
+}
+
 // The conversions between float64 and the fixed-point scale run on integer arithmetic over the
 // bits of the doubles: GB300's FP64 pipe made the plain double versions (ldexp, rounding,
 // subtraction, int64 <-> double conversions) the most expensive kernels of a solve.
@@ -560,9 +616,17 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_residual
     RG_CUDA(cudaMemsetAsync(sumsq, 0, sizeof(double), st));
     Grid g{n0, n1, n2};
     const uint64_t bytes = uint64_t(n0 * n1 * n2) * (16 + (Frem ? 4 : 0) + (r32 ? 4 : 0));
+    const bool rows_form = n2 % 2 == 0 && reinterpret_cast<uintptr_t>(U) % 16 == 0 &&
+                           reinterpret_cast<uintptr_t>(F) % 16 == 0 && reinterpret_cast<uintptr_t>(Frem) % 8 == 0 &&
+                           reinterpret_cast<uintptr_t>(r32) % 8 == 0;
     rg::profiled_launch("poisson_residual_fx", bytes, st, [&] {
-      fx_residual_kernel<<<grid3(g), 256, 0, st>>>(reinterpret_cast<const long long *>(U),
-                                                   reinterpret_cast<const long long *>(F), Frem, r32, g, e, k, sumsq);
+      if (rows_form)
+        fx_residual_rows_kernel<<<grid_rows(g, 8), 256, 0, st>>>(reinterpret_cast<const long long *>(U),
+                                                                 reinterpret_cast<const long long *>(F), Frem, r32,
+                                                                 g, e, k, sumsq);
+      else
+        fx_residual_kernel<<<grid3(g), 256, 0, st>>>(reinterpret_cast<const long long *>(U),
+                                                     reinterpret_cast<const long long *>(F), Frem, r32, g, e, k, sumsq);
     });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());

@@ -97,3 +97,36 @@ def test_fixed_point_conversions_bit_exact(rg, cuda):
     S = P.NeumannPoisson((4, 4, 4))
     for x in (f, f.astype(np.float32)):
         assert S.absmax(torch.from_numpy(x).cuda()) == float(np.abs(x).max())
+
+
+@pytest.mark.parametrize("shape", [(6, 5, 8), (6, 5, 7), (3, 4, 1030)])
+def test_fixed_point_residual_exact(rg, cuda, shape):
+    """R = F - A U of the 7-point Neumann stencil in int64 (modulo 2^64, exact for the small
+    results), r = R 2^-e + Frem as float and sum((r 2^-k)^2) 2^2k: the row-sweep form (even n2,
+    two elements per thread) and the one-element form (odd n2) against numpy's exact integers."""
+    torch = cuda
+    import ctypes
+
+    P = importlib.import_module("rocket_fft_gb300.poisson")
+    lib = P._bind()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(sum(shape))
+    U = rng.integers(-2**58, 2**58, shape, dtype=np.int64)
+    # F close to A U, so that R is small, as in the solver
+    pad = np.pad(U, 1, mode="edge").astype(object)
+    n0, n1, n2 = shape
+    AU = (pad[:-2, 1:-1, 1:-1] + pad[2:, 1:-1, 1:-1] + pad[1:-1, :-2, 1:-1] + pad[1:-1, 2:, 1:-1]
+          + pad[1:-1, 1:-1, :-2] + pad[1:-1, 1:-1, 2:] - 6 * U.astype(object))
+    R = rng.integers(-2**40, 2**40, shape, dtype=np.int64)
+    F = (AU + R.astype(object)).astype(np.int64)
+    Frem = (rng.standard_normal(shape) * 1e-3).astype(np.float32)
+    e, k = 30, 3
+    Ud, Fd, Frd = (torch.from_numpy(a).cuda() for a in (U, F, Frem))
+    r32 = torch.empty(shape, dtype=torch.float32, device="cuda")
+    ss = torch.empty(1, dtype=torch.float64, device="cuda")
+    assert lib.rocketgpu_poisson_residual_fx(Ud.data_ptr(), Fd.data_ptr(), Frd.data_ptr(), e, k, r32.data_ptr(),
+                                             n0, n1, n2, ss.data_ptr(), st) == 0
+    want = np.ldexp(R.astype(np.float64), -e) + Frem.astype(np.float64)
+    got = r32.cpu().numpy().astype(np.float64)
+    assert np.abs(got - want).max() <= 1e-6 * np.abs(want).max()
+    assert abs(float(ss.item()) - float(np.sum(want * want))) <= 1e-5 * float(np.sum(want * want))
