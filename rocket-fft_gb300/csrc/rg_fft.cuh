@@ -72,6 +72,14 @@ constexpr double kSqrtHalf = 0.7071067811865476;
 constexpr double kCos8 = 0.9238795325112867;  // cos(pi/8)
 constexpr double kSin8 = 0.3826834323650898;  // sin(pi/8)
 
+// cos(pi s / 16) and sin(pi s / 16), 1 <= s <= 7, correctly rounded to double
+__host__ __device__ __forceinline__ constexpr double kc16(int s) {
+  return s == 1 ? 0.9807852804032304 : s == 2 ? 0.9238795325112867 : s == 3 ? 0.8314696123025452
+       : s == 4 ? 0.7071067811865476 : s == 5 ? 0.5555702330196022 : s == 6 ? 0.3826834323650898
+       : 0.19509032201612828;
+}
+__host__ __device__ __forceinline__ constexpr double ks16(int s) { return kc16(8 - s); }
+
 template <typename T> __host__ __device__ __forceinline__ void dft4(cx<T> &a0, cx<T> &a1, cx<T> &a2, cx<T> &a3) {
   cx<T> t0 = add<T>(a0, a2), t1 = sub<T>(a0, a2), t2 = add<T>(a1, a3), t3 = mnegi<T>(sub<T>(a1, a3));
   a0 = add<T>(t0, t2);
@@ -90,6 +98,28 @@ template <typename T, int E> __host__ __device__ __forceinline__ cx<T> w16(cx<T>
   else if constexpr (E == 4) return mnegi<T>(a);                                      // -i
   else if constexpr (E == 6) return mk<T>((a.y - a.x) * r, -(a.x + a.y) * r);       // (-r, -r)
   else return mk<T>(-a.x * c - a.y * s, a.x * s - a.y * c);                         // E == 9: (-c, s)
+}
+
+// multiply by W_32^S = cos(pi S / 16) - i sin(pi S / 16), 0 <= S < 16
+template <typename T, int S> __host__ __device__ __forceinline__ cx<T> w32(cx<T> a) {
+  if constexpr (S == 0) {
+    return a;
+  } else if constexpr (S == 8) {
+    return mnegi<T>(a);
+  } else {
+    constexpr double c = S < 8 ? kc16(S) : -kc16(16 - S);
+    constexpr double sn = S < 8 ? ks16(S) : ks16(16 - S);
+    return mk<T>(a.x * T(c) + a.y * T(sn), a.y * T(c) - a.x * T(sn));
+  }
+}
+// the radix-2 combination of a 32-point DFT: y_s = e_s + W_32^s o_s, y_{s+16} = e_s - W_32^s o_s
+template <typename T, int S> __host__ __device__ __forceinline__ void dft32_join(cx<T> *v, const cx<T> *e, const cx<T> *o) {
+  if constexpr (S < 16) {
+    const cx<T> t = w32<T, S>(o[S]);
+    v[S] = add<T>(e[S], t);
+    v[S + 16] = sub<T>(e[S], t);
+    dft32_join<T, S + 1>(v, e, o);
+  }
 }
 
 template <typename T, int R> __host__ __device__ __forceinline__ void dft_odd(cx<T> *v) {
@@ -171,6 +201,17 @@ template <typename T, int R> __host__ __device__ __forceinline__ void dft(cx<T> 
     t = v[6]; v[6] = v[9]; v[9] = t;
     t = v[7]; v[7] = v[13]; v[13] = t;
     t = v[11]; v[11] = v[14]; v[14] = t;
+  } else if constexpr (R == 32) {
+    // even and odd points through two 16-point DFTs, then one radix-2 step
+    cx<T> e[16], o[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      e[j] = v[2 * j];
+      o[j] = v[2 * j + 1];
+    }
+    dft<T, 16>(e);
+    dft<T, 16>(o);
+    dft32_join<T, 0>(v, e, o);
   } else {
     dft_odd<T, R>(v);
   }

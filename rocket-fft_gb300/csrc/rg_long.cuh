@@ -12,8 +12,9 @@
 //
 // A phase-A tile is C = TT / n1 adjacent columns of one transform (its HBM reads are C-element
 // segments: lanes run across the columns first); a phase-B tile is D = TT / n2 adjacent rows of
-// Y (its HBM writes are D-element segments). Each thread runs one radix butterfly per pass (at
-// most 64 registers, two CTAs of TT / 16 threads per SM). Both phases read their first radix
+// Y (its HBM writes are D-element segments). Each thread runs one first-pass butterfly (radix
+// 16, at most 64 registers, TT / 16 threads; radix 32 for phases of 2^9 and 2^10 points, at most
+// 128 registers, TT / 32 threads) and the later passes' butterflies in turn. Both phases read their first radix
 // pass straight from global memory into registers and write their last pass straight back; the
 // passes in between run in place in one shared buffer, whose line pitch and padding period are
 // chosen at compile time to minimise shared-memory wavefronts over the kernel's access patterns.
@@ -159,22 +160,41 @@ constexpr int wave(const int (&slot)[32]) {
   }
   return total;
 }
-constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps) {
-  const int L = 1 << E, NP = fx::np_of(E);
+// Radix schedule of a phase of length 2^E: r0 = 16, the on-chip kernels' schedule (radix-16
+// passes, the last one 16, 8, 4 or 2); r0 = 32 (E = 8 .. 10): two passes, 32 x 2^(E-5).
+constexpr int np(int E, int r0) { return r0 == 32 ? 2 : fx::np_of(E); }
+constexpr int radix(int E, int r0, int p) { return r0 == 32 ? (p == 0 ? 32 : (1 << E) / 32) : fx::radix_of(E, p); }
+constexpr int ns(int E, int r0, int p) { return r0 == 32 ? (p == 0 ? 1 : 32) : fx::ns_of(E, p); }
+// offset of pass p's twiddles in the phase's table (r0 = 32: the table of get_pass_tw)
+constexpr int twoff(int E, int r0, int p) { return r0 == 32 ? 0 : fx::tw_of(E, p); }
+// First-pass radix of a shape: 32 when both phase lengths are 2^RG_LONG_R32_MIN .. 2^10, else
+// 16. For 2^9 and 2^10 the 32 x 2^(E-5) schedule has two passes instead of three (one
+// shared-memory round trip and two barriers fewer per tile): measured on GB300, c2c 2^18 .. 2^20
+// +11 %, r2c 2^21 +6 %. Taking 2^8 phases as 32 x 8 too (same pass count) measured -3 to -8 %
+// except c2c 2^17 (+4 %), so the default range starts at 2^9.
+#ifndef RG_LONG_R32_MIN
+#define RG_LONG_R32_MIN 9
+#endif
+constexpr int first_radix(int E1, int E2) {
+  return E1 >= RG_LONG_R32_MIN && E1 <= 10 && E2 >= RG_LONG_R32_MIN && E2 <= 10 ? 32 : 16;
+}
+
+constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, int r0) {
+  const int L = 1 << E, NP = np(E, r0);
   int total = 0;
   for (int w = 0; w < NT / 32 && w < 4; ++w) {
     int slot[32] = {};
-    // first pass (radix 16, output position 16 j + k)
-    for (int k = 0; k < 16; ++k) {
+    // first pass (radix r0, output position r0 j + k)
+    for (int k = 0; k < r0; ++k) {
       for (int l = 0; l < 32; ++l) {
         const int u = 32 * w + l;
-        const int line = a_side ? u % M : u / (L / 16), j = a_side ? u / M : u % (L / 16);
-        slot[l] = line * pitch + spad(16 * j + k, ps);
+        const int line = a_side ? u % M : u / (L / r0), j = a_side ? u / M : u % (L / r0);
+        slot[l] = line * pitch + spad(r0 * j + k, ps);
       }
       total += wave(slot);
     }
     for (int p = 1; p < NP; ++p) {
-      const int R = fx::radix_of(E, p), LR = L / R, NS = fx::ns_of(E, p);
+      const int R = radix(E, r0, p), LR = L / R, NS = ns(E, r0, p);
       for (int it = 0; it < (M * LR) / NT; ++it)
         for (int k = 0; k < R; ++k) {
           for (int l = 0; l < 32; ++l) {  // reads
@@ -199,11 +219,11 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps) 
 }
 // For padding period 2^ps: the pitch (>= the padded line length, within 16 slots of it) with
 // the fewest wavefronts, as cost * 2^16 + pitch.
-constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps) {
+constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps, int r0) {
   const int base = spad((1 << E) - 1, ps) + 1;
   int best = base, cost = 1 << 14;
   for (int p = base; p < base + 16; ++p) {
-    const int c = phase_waves(E, M, NT, p, a_side, ps);
+    const int c = phase_waves(E, M, NT, p, a_side, ps, r0);
     if (c < cost) {
       cost = c;
       best = p;
@@ -225,35 +245,39 @@ constexpr int pick_layout(int c5, int c4, int c3) {
 template <int E1, int E2, int ET> struct LgCfg {
   static constexpr int N1 = 1 << E1, N2 = 1 << E2, TT = 1 << ET;
   static constexpr int C = TT / N1, D = TT / N2;  // columns per A tile, rows per B tile
-  static constexpr int NT = TT / 16;              // threads: one radix-16 butterfly each
+  static constexpr int R0 = lg::first_radix(E1, E2);
+  static constexpr int NT = TT / R0;              // threads: one first-pass butterfly each
+  // CTAs per SM the registers are sized for: 64 registers a thread at 16 points per thread, 128
+  // at 32
+  static constexpr int MINB = R0 == 32 ? 512 / NT : 1024 / NT;
   // shared layout of each phase: padding period and line pitch (each candidate period searched
   // in a constant of its own, within the compiler's constant-evaluation budget)
-  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5), A4 = lg::best_pitch(E1, C, NT, true, 4);
-  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3);
-  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5), B4 = lg::best_pitch(E2, D, NT, false, 4);
-  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3);
+  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5, R0), A4 = lg::best_pitch(E1, C, NT, true, 4, R0);
+  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3, R0);
+  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5, R0), B4 = lg::best_pitch(E2, D, NT, false, 4, R0);
+  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3, R0);
   static constexpr int LA = lg::pick_layout(A5, A4, A3), LB = lg::pick_layout(B5, B4, B3);
   static constexpr int PA = LA & 0xffff, PB = LB & 0xffff;  // line pitches (slots)
   static constexpr int SA = LA >> 16, SB = LB >> 16;        // padding periods (log2)
   static constexpr int SLOTS = C * PA > D * PB ? C * PA : D * PB;
   // radix of phase A's last pass, and its per-tile factors W_n^{col k NS} (k = 1 .. RA-1, one
   // per column of the tile)
-  static constexpr int RA = fx::radix_of(E1, fx::np_of(E1) - 1);
+  static constexpr int RA = lg::radix(E1, R0, lg::np(E1, R0) - 1);
   static constexpr int FTAB = (RA - 1) * C;
   // the tile, the factor table, then two control words (ticket, wait failure): no static
   // shared memory, so the dynamic size may be raised to the device's opt-in maximum
   static constexpr size_t CTRL = size_t(SLOTS + FTAB) * 8;
   static constexpr size_t SMEM = CTRL + 16;
   static_assert(C >= 2 && D >= 2 && C <= 32 && D <= 32, "tile shape");
-  static_assert(fx::radix_of(E1, 0) == 16 && fx::radix_of(E2, 0) == 16, "first pass radix 16");
+  static_assert(lg::radix(E1, R0, 0) == R0 && lg::radix(E2, R0, 0) == R0, "first pass radix");
 };
 
 // ---- passes over lines of length 2^E held in shared memory (line l at sm + l * PITCH) ----
 
 // Middle pass P, in place: all butterflies read (and transform) before a barrier, then write.
-template <int E, int P, int M, int NT, int PITCH, int PS>
+template <int E, int R0, int P, int M, int NT, int PITCH, int PS>
 __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__ tw) {
-  constexpr int L = 1 << E, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P), TWO = fx::tw_of(E, P);
+  constexpr int L = 1 << E, R = lg::radix(E, R0, P), LR = L / R, NS = lg::ns(E, R0, P), TWO = lg::twoff(E, R0, P);
   constexpr int UNITS = M * LR, ITER = (UNITS + NT - 1) / NT;
   static_assert(UNITS % NT == 0, "whole iterations");
   float2 v[ITER][R];
@@ -284,21 +308,21 @@ __device__ __forceinline__ void lg_middle(float2 *sm, const float2 *__restrict__
   __syncthreads();
 }
 
-template <int E, int M, int NT, int PITCH, int PS, int P, int PEND>
+template <int E, int R0, int M, int NT, int PITCH, int PS, int P, int PEND>
 __device__ __forceinline__ void lg_middles(float2 *sm, const float2 *__restrict__ tw) {
   if constexpr (P < PEND) {
-    lg_middle<E, P, M, NT, PITCH, PS>(sm, tw);
-    lg_middles<E, M, NT, PITCH, PS, P + 1, PEND>(sm, tw);
+    lg_middle<E, R0, P, M, NT, PITCH, PS>(sm, tw);
+    lg_middles<E, R0, M, NT, PITCH, PS, P + 1, PEND>(sm, tw);
   }
 }
 
 // Last-pass butterfly j of line l: inputs from shared memory, twiddled, transformed; output k
 // lands at position j + k * NS of the transform.
-template <int E, int PITCH, int PS>
+template <int E, int R0, int PITCH, int PS>
 __device__ __forceinline__ void lg_last_one(const float2 *sm, const float2 *__restrict__ tw, int l, int j,
-                                            float2 (&a)[fx::radix_of(E, fx::np_of(E) - 1)]) {
-  constexpr int L = 1 << E, P = fx::np_of(E) - 1, R = fx::radix_of(E, P), LR = L / R, NS = fx::ns_of(E, P);
-  constexpr int TWO = fx::tw_of(E, P);
+                                            float2 (&a)[lg::radix(E, R0, lg::np(E, R0) - 1)]) {
+  constexpr int L = 1 << E, P = lg::np(E, R0) - 1, R = lg::radix(E, R0, P), LR = L / R, NS = lg::ns(E, R0, P);
+  constexpr int TWO = lg::twoff(E, R0, P);
   static_assert(NS == LR, "last pass");
   const float2 *s0 = sm + l * PITCH;
 #pragma unroll
@@ -368,7 +392,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
   // pass's barrier.
   float2 *ftab = sm + Cf::SLOTS;
   {
-    constexpr int NS = N1 / Cf::RA;
+    constexpr int NS = N1 / Cf::RA;  // the last pass's stride (= its butterflies per line)
     for (int i = int(threadIdx.x); i < Cf::FTAB; i += NT) {
       const int kk = i / C + 1, cc = i - (kk - 1) * C;
       const int col = KIND == LG_C2R ? pair_index<N2, C>(part, cc) : part * C + cc;
@@ -376,8 +400,8 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     }
   }
   if constexpr (KIND != LG_C2R) {
-    // first pass: radix 16 straight from global memory; lanes run across the C columns first
-    constexpr int R = 16, LR = N1 / R, UNITS = C * LR;
+    // first pass: radix R0 straight from global memory; lanes run across the C columns first
+    constexpr int R = Cf::R0, LR = N1 / R, UNITS = C * LR;
     static_assert(UNITS == NT, "one unit per thread");
     const int u = int(threadIdx.x);
     const int c = u % C, j = u / C;
@@ -396,7 +420,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) l0[lg::sp_k<1, SA>(j * R, k)] = v[k];
     __syncthreads();
-    lg_middles<E1, C, NT, PA, SA, 1, fx::np_of(E1) - 1>(sm, tw);
+    lg_middles<E1, Cf::R0, C, NT, PA, SA, 1, lg::np(E1, Cf::R0) - 1>(sm, tw);
   } else {
     // c2r: merge the half spectrum X (m + 1 elements, m = n1 n2) of columns j2 and n2 - j2
     // into conj(Z) on chip, then every pass but the last in shared memory
@@ -432,12 +456,12 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     }
     if (t == 0 && threadIdx.x == 0) merge(0, N1 / 2, 0, N1 / 2, M / 2, false);
     __syncthreads();
-    lg_middles<E1, C, NT, PA, SA, 0, fx::np_of(E1) - 1>(sm, tw);
+    lg_middles<E1, Cf::R0, C, NT, PA, SA, 0, lg::np(E1, Cf::R0) - 1>(sm, tw);
   }
   // last pass: outputs k1 = j + k * NS, times W_n^{j2 k1}, to Y[k1][j2]; lanes across the C
   // columns first (L2-resident stores, kept there with an evict-last policy)
   {
-    constexpr int P = fx::np_of(E1) - 1, R = fx::radix_of(E1, P), LR = N1 / R, NS = LR;
+    constexpr int P = lg::np(E1, Cf::R0) - 1, R = lg::radix(E1, Cf::R0, P), LR = N1 / R, NS = LR;
     constexpr int UNITS = C * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
     static_assert(R == Cf::RA, "factor table radix");
@@ -447,7 +471,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       const int u = int(threadIdx.x) + it * NT;
       const int c = u % C, j = u / C;
       float2 v[R];
-      lg_last_one<E1, PA, SA>(sm, tw, c, j, v);
+      lg_last_one<E1, Cf::R0, PA, SA>(sm, tw, c, j, v);
       const int col = KIND == LG_C2R ? pair_index<N2, C>(part, c) : part * C + c;
       float2 *yc = y + col;
       const float2 wj = split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * uint32_t(j));
@@ -474,9 +498,9 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     const int k1 = KIND == LG_R2C ? pair_index<N1, D>(part, r) : part * D + r;
     return yg + int64_t(k1) * N2;
   };
-  // first pass: radix 16 from Y (L2); lanes along the row
+  // first pass: radix R0 from Y (L2); lanes along the row
   {
-    constexpr int R = 16, LR = N2 / R, UNITS = D * LR;
+    constexpr int R = Cf::R0, LR = N2 / R, UNITS = D * LR;
     static_assert(UNITS == NT, "one unit per thread");
     const int u = int(threadIdx.x);
     const int r = u / LR, j = u % LR;
@@ -500,9 +524,9 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
   const float sgn = a.conj_out ? -fct : fct;
   const uint64_t pol = input_policy((a.flags & kLongEvictOut) != 0);
   if constexpr (KIND != LG_R2C) {
-    lg_middles<E2, D, NT, PB, SB, 1, fx::np_of(E2) - 1>(sm, tw);
+    lg_middles<E2, Cf::R0, D, NT, PB, SB, 1, lg::np(E2, Cf::R0) - 1>(sm, tw);
     // last pass: outputs k2 = j + k * NS of row r to X[r + k2 n1]; lanes across the D rows first
-    constexpr int P = fx::np_of(E2) - 1, R = fx::radix_of(E2, P), LR = N2 / R, NS = LR;
+    constexpr int P = lg::np(E2, Cf::R0) - 1, R = lg::radix(E2, Cf::R0, P), LR = N2 / R, NS = LR;
     constexpr int UNITS = D * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
     float2 *Xt = X + part * D;
@@ -511,7 +535,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
       const int u = int(threadIdx.x) + it * NT;
       const int r = u % D, j = u / D;
       float2 v[R];
-      lg_last_one<E2, PB, SB>(sm, tw, r, j, v);
+      lg_last_one<E2, Cf::R0, PB, SB>(sm, tw, r, j, v);
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const int64_t k2 = j + k * NS;
@@ -520,7 +544,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     }
   } else {
     // r2c: every pass on chip, then the split of each row pair into X_k and X_{m-k}
-    lg_middles<E2, D, NT, PB, SB, 1, fx::np_of(E2)>(sm, tw);
+    lg_middles<E2, Cf::R0, D, NT, PB, SB, 1, lg::np(E2, Cf::R0)>(sm, tw);
     constexpr int64_t M = int64_t(N1) * N2;
     constexpr int H = D / 2;
     const float2 *lo2 = reinterpret_cast<const float2 *>(a.lo2), *hi2 = reinterpret_cast<const float2 *>(a.hi2);
@@ -572,7 +596,7 @@ __device__ __forceinline__ void red_release_add(int *p, int v) {
 // KIND: LG_C2C (complex in, complex out), LG_R2C (real in, n/2+1 complex out), LG_C2R. Row
 // offsets from the sides are in units of the side's element (float for real rows).
 template <int KIND, int E1, int E2, int ET>
-__global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, 1024 / LgCfg<E1, E2, ET>::NT)
+__global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, LgCfg<E1, E2, ET>::MINB)
     long_kernel(const __grid_constant__ LongArgs a) {
   using Cf = LgCfg<E1, E2, ET>;
   constexpr int64_t n = int64_t(1) << (E1 + E2);

@@ -254,6 +254,22 @@ const void *get_roots(uint64_t n, uint64_t count, DType dt) {
   return r->d;
 }
 
+const void *get_pass_tw(int L, int R0, DType dt) {
+  struct Tw {
+    const void *d;
+  };
+  Key k{current_device(), int(dt), 5, uint64_t(L), uint64_t(R0)};
+  auto r = cached<Tw>(k, [&](Tw &o, Entry &e) {
+    std::vector<std::complex<double>> v;
+    for (int kk = 1; kk < L / R0; ++kk)
+      for (int m = 0; m < R0; ++m) v.push_back(wfwd(uint64_t(m) * kk, uint64_t(L)));
+    void *d = upload(v, dt, e.bytes);
+    e.dptrs.push_back(d);
+    o.d = d;
+  });
+  return r->d;
+}
+
 SplitTables get_split(uint64_t N, DType dt) {
   Key k{current_device(), int(dt), 3, N, 0};
   auto r = cached<SplitTables>(k, [&](SplitTables &o, Entry &e) {

@@ -40,6 +40,10 @@ const CoreTables &get_core(int L, DType dt);
 // W_n^k (forward sign) for k = 0..count-1
 const void *get_roots(uint64_t n, uint64_t count, DType dt);
 
+// Twiddles of the second pass of the two-pass schedule R0 x L / R0: entry (k - 1) R0 + m is
+// W_L^{m k} (m < R0, 1 <= k < L / R0), the layout of a core table's pass with Ns = R0.
+const void *get_pass_tw(int L, int R0, DType dt);
+
 struct SplitTables {
   const void *lo, *hi;
   int shift;
