@@ -101,6 +101,10 @@ void run_long(int64_t m, const void *in, const Side &ld, void *out, const Side &
   const int64_t G = std::max<int64_t>(1, std::min<int64_t>(nrows, want / ybytes));
   const int64_t ng = (nrows + G - 1) / G;
   int64_t nbuf = std::max<int64_t>(1, std::min<int64_t>(8, budget / (G * ybytes)));
+  // one group of 64 MiB (2^23 complex points) fills the default ring: a second slot up to a
+  // 128 MiB ring lets phase A of the next transform overlap phase B of this one (measured on
+  // GB300: c2c 2^23 and r2c 2^24 +10-11 %)
+  if (nbuf < 2 && !std::getenv("ROCKET_GPU_LONG_YMB") && 2 * G * ybytes <= (int64_t(128) << 20)) nbuf = 2;
   const int nenv = env_int("ROCKET_GPU_LONG_NBUF", 0);
   if (nenv >= 1 && nenv <= 16) nbuf = nenv;
   nbuf = std::min<int64_t>(nbuf, ng);
