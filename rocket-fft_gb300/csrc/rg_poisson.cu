@@ -539,19 +539,23 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_eigdiv(v
     RG_CHECK(n0 > 0 && n1 > 0 && n2 > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Grid g{n0, n1, n2};
-    const unsigned b = grid_rows(g, 4);
     const uint64_t bytes = uint64_t(2 * itemsize) * uint64_t(n0 * n1 * n2);
+    // vector rows: n2 a multiple of the vector width and X 16-byte aligned
+    const bool vec = n2 % (16 / itemsize) == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0;
+    // threads: one per vector of a row (a multiple of 32, at most 256), so that none idles on
+    // short rows (512 float32 points: 128 threads), and CTAs per SM in proportion
+    const int64_t per_row = (n2 / (vec ? 16 / itemsize : 1) + 31) / 32 * 32;
+    const int threads = int(std::min<int64_t>(256, std::max<int64_t>(32, per_row)));
+    const unsigned b = grid_rows(g, 4 * 256 / threads);
     rg::profiled_launch(itemsize == 4 ? "poisson_eigdiv_f32" : "poisson_eigdiv_f64", bytes, st, [&] {
-      // vector rows: n2 a multiple of the vector width and X 16-byte aligned
-      const bool vec = n2 % (16 / itemsize) == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0;
       if (itemsize == 4) {
         const float *l = static_cast<const float *>(lam);
-        if (vec) eigdiv_kernel<float, 4><<<b, 256, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
-        else eigdiv_kernel<float, 1><<<b, 256, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
+        if (vec) eigdiv_kernel<float, 4><<<b, threads, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
+        else eigdiv_kernel<float, 1><<<b, threads, 0, st>>>(static_cast<float *>(X), g, l, l + n0, l + n0 + n1);
       } else {
         const double *l = static_cast<const double *>(lam);
-        if (vec) eigdiv_kernel<double, 2><<<b, 256, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
-        else eigdiv_kernel<double, 1><<<b, 256, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
+        if (vec) eigdiv_kernel<double, 2><<<b, threads, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
+        else eigdiv_kernel<double, 1><<<b, threads, 0, st>>>(static_cast<double *>(X), g, l, l + n0, l + n0 + n1);
       }
     });
     rg::note_launch();
