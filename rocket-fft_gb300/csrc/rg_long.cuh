@@ -13,11 +13,13 @@
 // A phase-A tile is C = TT / n1 adjacent columns of one transform (its HBM reads are C-element
 // segments: lanes run across the columns first); a phase-B tile is D = TT / n2 adjacent rows of
 // Y (its HBM writes are D-element segments). Each thread runs one first-pass butterfly (radix
-// 16, at most 64 registers, TT / 16 threads; radix 32 for phases of 2^9 and 2^10 points, at most
-// 128 registers, TT / 32 threads) and the later passes' butterflies in turn. Both phases read their first radix
-// pass straight from global memory into registers and write their last pass straight back; the
-// passes in between run in place in one shared buffer, whose line pitch and padding period are
-// chosen at compile time to minimise shared-memory wavefronts over the kernel's access patterns.
+// 16, at most 64 registers, TT / 16 threads; radix 32 when both phases are 2^9 or 2^10 points,
+// at most 128 registers, TT / 32 threads) and the later passes' butterflies in turn. Both phases
+// read their first radix pass straight from global memory into registers and write their last
+// pass straight back; the passes in between run in place in one shared buffer, whose line pitch
+// and padding period are chosen at compile time to minimise shared-memory wavefronts over the
+// kernel's access patterns. Phase A's four-step twiddle is a per-butterfly table lookup times a
+// factor from a per-tile table in shared memory.
 //
 // Y is the only intermediate, and it is kept in L2: transforms go through in groups of G
 // (G * n * 8 bytes of Y per group), and group g uses slot g mod S of a ring of S Y buffers.
