@@ -280,6 +280,59 @@ __global__ void __launch_bounds__(256) fx_residual_rows_kernel(const long long *
   }
 }
 
+// Sliding-window form, for rows of 64 .. 512 points (a multiple of 64): a CTA of n2 / 2 threads
+// (two adjacent points each) walks a strip of STRIP rows k1 of one plane k0 and keeps the U values
+// of rows k1 - 1, k1 and k1 + 1 in registers; the neighbours along the row come from the
+// adjacent lanes by shuffles (a warp's edge lanes load theirs). Each U row is then read three
+// times (its own plane's walk and the two neighbouring planes'), not seven. CTAs go through the
+// planes in order, so the neighbouring planes' rows are recent L2 lines.
+template <int STRIP>
+__global__ void __launch_bounds__(256) fx_residual_window_kernel(const long long *U, const long long *F,
+                                                                 const float *Frem, float *r32, Grid g, int e, int k,
+                                                                 double *sum) {
+  typedef unsigned long long u64;
+  const int64_t s0 = g.n1 * g.n2, s1 = g.n2;
+  const int64_t strips = (g.n1 + STRIP - 1) / STRIP;
+  const int64_t k0 = int64_t(blockIdx.x) / strips, k1a = (int64_t(blockIdx.x) - k0 * strips) * STRIP;
+  const int64_t k1b = k1a + STRIP < g.n1 ? k1a + STRIP : g.n1;
+  const int64_t k2 = 2 * int64_t(threadIdx.x);  // n2 == 2 * blockDim.x
+  const int64_t o0m = k0 > 0 ? -s0 : 0, o0p = k0 + 1 < g.n0 ? s0 : 0;
+  const int64_t plane = k0 * s0 + k2;
+  const unsigned lane = threadIdx.x & 31u;
+  auto ldU = [&](int64_t r) { return *reinterpret_cast<const longlong2 *>(U + plane + r * s1); };
+  longlong2 prev = ldU(k1a > 0 ? k1a - 1 : k1a), cur = ldU(k1a);
+  float acc = 0.f;
+  for (int64_t k1 = k1a; k1 < k1b; ++k1) {
+    const int64_t i = plane + k1 * s1;
+    const longlong2 next = ldU(k1 + 1 < g.n1 ? k1 + 1 : k1);
+    const longlong2 m0 = *reinterpret_cast<const longlong2 *>(U + i + o0m);
+    const longlong2 p0 = *reinterpret_cast<const longlong2 *>(U + i + o0p);
+    const longlong2 f = *reinterpret_cast<const longlong2 *>(F + i);
+    const float2 fr = Frem ? *reinterpret_cast<const float2 *>(Frem + i) : make_float2(0.f, 0.f);
+    long long left = __shfl_up_sync(0xffffffffu, cur.y, 1);
+    long long right = __shfl_down_sync(0xffffffffu, cur.x, 1);
+    if (lane == 0) left = k2 > 0 ? U[i - 1] : cur.x;
+    if (lane == 31) right = k2 + 2 < g.n2 ? U[i + 2] : cur.y;
+    const u64 nx = ((u64)m0.x + (u64)p0.x) + ((u64)prev.x + (u64)next.x) + ((u64)left + (u64)cur.y);
+    const u64 ny = ((u64)m0.y + (u64)p0.y) + ((u64)prev.y + (u64)next.y) + ((u64)cur.x + (u64)right);
+    const float rx = fx_res_one((u64)cur.x, nx, f.x, fr.x, e), ry = fx_res_one((u64)cur.y, ny, f.y, fr.y, e);
+    if (r32) *reinterpret_cast<float2 *>(r32 + i) = make_float2(rx, ry);
+    const float sx = ldexpf(rx, -k), sy = ldexpf(ry, -k);
+    acc = fmaf(sx, sx, fmaf(sy, sy, acc));
+    prev = cur;
+    cur = next;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ float red[8];
+  if (lane == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += double(red[w]);
+    atomicAdd(sum, std::ldexp(t, 2 * k));
+  }
+}
+
 // The conversions between float64 and the fixed-point scale run on integer arithmetic over the
 // bits of the doubles: GB300's FP64 pipe made the plain double versions (ldexp, rounding,
 // subtraction, int64 <-> double conversions) the most expensive kernels of a solve.
@@ -623,8 +676,13 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_residual
     const bool rows_form = n2 % 2 == 0 && reinterpret_cast<uintptr_t>(U) % 16 == 0 &&
                            reinterpret_cast<uintptr_t>(F) % 16 == 0 && reinterpret_cast<uintptr_t>(Frem) % 8 == 0 &&
                            reinterpret_cast<uintptr_t>(r32) % 8 == 0;
+    constexpr int kStrip = 32;
+    const bool window_form = rows_form && n2 % 64 == 0 && n2 <= 512 && n0 * ((n1 + kStrip - 1) / kStrip) < (int64_t(1) << 31);
     rg::profiled_launch("poisson_residual_fx", bytes, st, [&] {
-      if (rows_form)
+      if (window_form)
+        fx_residual_window_kernel<kStrip><<<unsigned(n0 * ((n1 + kStrip - 1) / kStrip)), unsigned(n2 / 2), 0, st>>>(
+            reinterpret_cast<const long long *>(U), reinterpret_cast<const long long *>(F), Frem, r32, g, e, k, sumsq);
+      else if (rows_form)
         fx_residual_rows_kernel<<<grid_rows(g, 8), 256, 0, st>>>(reinterpret_cast<const long long *>(U),
                                                                  reinterpret_cast<const long long *>(F), Frem, r32,
                                                                  g, e, k, sumsq);

@@ -99,11 +99,12 @@ def test_fixed_point_conversions_bit_exact(rg, cuda):
         assert S.absmax(torch.from_numpy(x).cuda()) == float(np.abs(x).max())
 
 
-@pytest.mark.parametrize("shape", [(6, 5, 8), (6, 5, 7), (3, 4, 1030)])
+@pytest.mark.parametrize("shape", [(6, 5, 8), (6, 5, 7), (3, 4, 1030), (5, 7, 64), (4, 70, 128), (3, 33, 512)])
 def test_fixed_point_residual_exact(rg, cuda, shape):
     """R = F - A U of the 7-point Neumann stencil in int64 (modulo 2^64, exact for the small
-    results), r = R 2^-e + Frem as float and sum((r 2^-k)^2) 2^2k: the row-sweep form (even n2,
-    two elements per thread) and the one-element form (odd n2) against numpy's exact integers."""
+    results), r = R 2^-e + Frem as float and sum((r 2^-k)^2) 2^2k: the sliding-window form (n2 a
+    multiple of 64 up to 512, strips of 32 rows), the row-sweep form (other even n2, two elements
+    per thread) and the one-element form (odd n2) against numpy's exact integers."""
     torch = cuda
     import ctypes
 
