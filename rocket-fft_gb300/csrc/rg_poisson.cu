@@ -33,6 +33,11 @@ struct Grid {
   int64_t n0, n1, n2;
 };
 
+// Elementwise kernels walk their arrays in grid-stride steps of kIlp elements per thread (at
+// i, i + stride, ...), all loads of a step issued before any use: with one load in flight per
+// thread the conversions ran at 0.26-0.6 of the HBM copy bandwidth (latency-bound).
+constexpr int kIlp = 4;
+
 // Row sweep of the n0 x n1 x n2 grid (C order) for the elementwise and stencil kernels: a few
 // CTAs per SM; at step t CTA b takes the ROWS rows (k0, k1) number t * G * ROWS + u * G + b
 // (u < ROWS, G = gridDim.x), its threads run along the last axis, and the loads of all ROWS rows
@@ -170,9 +175,21 @@ __global__ void __launch_bounds__(256) update_kernel(double *uh, float *ul, cons
 // U += round(delta * 2^e) (assign: U = round(delta * 2^e), the first correction)
 __global__ void __launch_bounds__(256) fx_update_kernel(long long *U, const float *delta, int64_t total, int e,
                                                         int assign) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    const long long d = __float2ll_rn(ldexpf(delta[i], e));
-    U[i] = assign ? d : U[i] + d;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < total; i0 += kIlp * stride) {
+    float d[kIlp];
+    long long u[kIlp];
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      d[q] = i < total ? delta[i] : 0.f;
+      u[q] = i < total && !assign ? U[i] : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      if (i < total) U[i] = u[q] + __float2ll_rn(ldexpf(d[q], e));
+    }
   }
 }
 
@@ -391,14 +408,34 @@ __device__ __forceinline__ void fixed_of(double f, int e, long long &F, float &r
 
 __global__ void __launch_bounds__(256) fx_from_double_kernel(const double *f, long long *F, float *Frem, int64_t total,
                                                              int e) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    long long v;
-    float rem;
-    fixed_of(f[i], e, v, rem);
-    F[i] = v;
-    if (Frem) Frem[i] = rem;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < total; i0 += kIlp * stride) {
+    double x[kIlp];
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      x[q] = i < total ? f[i] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      if (i < total) {
+        long long v;
+        float rem;
+        fixed_of(x[q], e, v, rem);
+        F[i] = v;
+        if (Frem) Frem[i] = rem;
+      }
+    }
   }
 }
+
+// The out-of-range fallbacks of the integer conversions below, kept out of line: inlined, the
+// compiler evaluated them for every element (predicated), which put an FP64 conversion per
+// element on GB300's FP64 pipe (85 % busy in the fixed-point to double conversion, 0.26 of the
+// HBM copy bandwidth).
+__device__ __noinline__ double scaled_double_slow(long long v, int e) { return ldexp(double(v), -e); }
+__device__ __noinline__ float float_of_slow(double f) { return __double2float_rn(f); }
 
 // v 2^-e as a double rounded to nearest even, assembled from the normalised magnitude of v
 // (no FP64 operations); results outside the normal range fall back to the double path.
@@ -417,7 +454,7 @@ __device__ __forceinline__ double scaled_double(long long v, int e) {
     ++E;
   }
   const int biased = E + 1023;
-  if (biased <= 0 || biased >= 2047) return ldexp(double(v), -e);
+  if (biased <= 0 || biased >= 2047) return scaled_double_slow(v, e);
   return __longlong_as_double((long long)(sgn | (unsigned long long)biased << 52 | (mant & 0xfffffffffffffull)));
 }
 
@@ -425,8 +462,20 @@ __device__ __forceinline__ double scaled_double(long long v, int e) {
 __global__ void __launch_bounds__(256) fx_to_double_kernel(const long long *U, double *out, int64_t total, int e,
                                                            const long long *m) {
   const long long shift = m ? *m : 0;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
-    out[i] = scaled_double(U[i] - shift, e);
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < total; i0 += kIlp * stride) {
+    long long v[kIlp];
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      v[q] = i < total ? U[i] : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      if (i < total) out[i] = scaled_double(v[q] - shift, e);
+    }
+  }
 }
 
 // Exact sum of the int64 iterate (128-bit accumulators), one partial per CTA.
@@ -466,11 +515,20 @@ __global__ void __launch_bounds__(256) absmax_kernel(const T *x, int64_t total, 
   using B = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned>::type;
   constexpr B mask = B(~B(0)) >> 1;
   B mx = 0;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    B b;
-    memcpy(&b, x + i, sizeof(B));
-    b &= mask;
-    mx = b > mx ? b : mx;
+  const B *xb = reinterpret_cast<const B *>(x);  // the bits of the values
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < total; i0 += kIlp * stride) {
+    B b[kIlp];
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      b[q] = i < total ? xb[i] : B(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const B c = b[q] & mask;
+      mx = c > mx ? c : mx;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     const B y = __shfl_down_sync(0xffffffffu, mx, o);
@@ -498,7 +556,7 @@ __global__ void __launch_bounds__(256) absmax_kernel(const T *x, int64_t total, 
 __device__ __forceinline__ float float_of(double f) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(f);
   const int E = int((b >> 52) & 0x7ffull) - 1023 + 127;
-  if (E <= 0 || E >= 254) return __double2float_rn(f);
+  if (E <= 0 || E >= 254) return float_of_slow(f);
   unsigned long long m = (b & 0xfffffffffffffull) >> 29;
   const unsigned long long rb = b & ((1ull << 29) - 1), half = 1ull << 28;
   unsigned e = unsigned(E);
@@ -516,13 +574,25 @@ __device__ __forceinline__ float float_of(double f) {
 __global__ void __launch_bounds__(256) prepare_kernel(const double *f, float *r32, int64_t total, double *stats) {
   unsigned long long mx = 0;
   float ss = 0.f;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    const double v = f[i];
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
-    mx = b > mx ? b : mx;
-    const float x = float_of(v);
-    r32[i] = x;
-    ss = fmaf(x, x, ss);
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < total; i0 += kIlp * stride) {
+    double v[kIlp];
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      v[q] = i < total ? f[i] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < kIlp; ++q) {
+      const int64_t i = i0 + q * stride;
+      if (i < total) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v[q]) & 0x7fffffffffffffffull;
+        mx = b > mx ? b : mx;
+        const float x = float_of(v[q]);
+        r32[i] = x;
+        ss = fmaf(x, x, ss);
+      }
+    }
   }
   double ssd = double(ss);
   for (int o = 16; o > 0; o >>= 1) {
@@ -700,7 +770,9 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_to_fx(co
   return guarded([&] {
     RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    fx_from_double_kernel<<<grid_for(total), 256, 0, st>>>(f, reinterpret_cast<long long *>(F), Frem, total, e);
+    rg::profiled_launch("poisson_to_fx", uint64_t(total) * 20, st, [&] {
+      fx_from_double_kernel<<<grid_for(total), 256, 0, st>>>(f, reinterpret_cast<long long *>(F), Frem, total, e);
+    });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
@@ -731,9 +803,11 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_fx_to_do
     unsigned long long *part = static_cast<unsigned long long *>(work.get());
     long long *m = reinterpret_cast<long long *>(part + 2 * g);
     const long long *u = reinterpret_cast<const long long *>(U);
-    fx_sum_kernel<<<g, 256, 0, st>>>(u, total, part);
+    rg::profiled_launch("poisson_fx_sum", uint64_t(total) * 8, st,
+                        [&] { fx_sum_kernel<<<g, 256, 0, st>>>(u, total, part); });
     fx_mean_kernel<<<1, 32, 0, st>>>(part, int(g), total, m);
-    fx_to_double_kernel<<<g, 256, 0, st>>>(u, out, total, e, m);
+    rg::profiled_launch("poisson_fx_to_double", uint64_t(total) * 16, st,
+                        [&] { fx_to_double_kernel<<<g, 256, 0, st>>>(u, out, total, e, m); });
     for (int i = 0; i < 3; ++i) rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
@@ -745,7 +819,9 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_init_fx(
   return guarded([&] {
     RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    fx_update_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<long long *>(U), delta, total, e, 1);
+    rg::profiled_launch("poisson_init_fx", uint64_t(total) * 12, st, [&] {
+      fx_update_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<long long *>(U), delta, total, e, 1);
+    });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
@@ -758,7 +834,8 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_prepare(
     RG_CHECK(total > 0, RG_ERR_ARG, "empty grid");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     RG_CUDA(cudaMemsetAsync(stats, 0, 2 * sizeof(double), st));
-    prepare_kernel<<<grid_for(total), 256, 0, st>>>(f, r32, total, stats);
+    rg::profiled_launch("poisson_prepare", uint64_t(total) * 12, st,
+                        [&] { prepare_kernel<<<grid_for(total), 256, 0, st>>>(f, r32, total, stats); });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
@@ -773,8 +850,10 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_abs_max(const vo
     RG_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
     if (total == 0) return;
     unsigned long long *o = reinterpret_cast<unsigned long long *>(out);
-    if (itemsize == 8) absmax_kernel<double><<<grid_for(total), 256, 0, st>>>(static_cast<const double *>(x), total, o);
-    else absmax_kernel<float><<<grid_for(total), 256, 0, st>>>(static_cast<const float *>(x), total, o);
+    rg::profiled_launch("abs_max", uint64_t(total) * uint64_t(itemsize), st, [&] {
+      if (itemsize == 8) absmax_kernel<double><<<grid_for(total), 256, 0, st>>>(static_cast<const double *>(x), total, o);
+      else absmax_kernel<float><<<grid_for(total), 256, 0, st>>>(static_cast<const float *>(x), total, o);
+    });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
   });
