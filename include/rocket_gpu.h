@@ -132,8 +132,9 @@ int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, ro
  * ghost cells); the DCT-II diagonalises the 7-point Laplacian with eigenvalues
  * lam0[k0] + lam1[k1] + lam2[k2], lam_a[k] = 2 cos(pi k / n_a) - 2.
  *   rocketgpu_poisson_eigdiv: X /= lambda in place (float or double, itemsize 4/8; the table lam =
- *     lam0|lam1|lam2 is in the same precision as X, arithmetic in that precision), mode 0 set
- *     to 0; lam = the three device tables back to back (n0+n1+n2 doubles).
+ *     lam0|lam1|lam2 is in the same precision as X, arithmetic in that precision: float32 by the
+ *     fast division, within two ulp), mode 0 set to 0; lam = the three device tables back to
+ *     back (n0+n1+n2 values).
  *   rocketgpu_poisson_update: u += delta with an exact two-sum whose rounding error goes to the
  *     float u_lo (u_lo may be NULL).
  *   rocketgpu_poisson_residual: r = f - A (u + u_lo) in double (u_lo may be NULL), written as
@@ -148,6 +149,13 @@ int rocketgpu_dct_adjoint_st(uint64_t ndim, const rocketgpu_arystruct_t *ain, ro
  * All return a status; rocketgpu_poisson_last_error gives the calling thread's message. */
 int rocketgpu_poisson_eigdiv(void *X, int64_t itemsize, int64_t n0, int64_t n1, int64_t n2, const void *lam,
                              void *stream);
+/* out = rocketgpu_poisson_eigdiv applied to the DCT-II (fct 1) of the float32 volume in over all
+ * three axes, the divide done by the last axis' pass as it stores (results identical to the two
+ * calls; in and out C-contiguous, distinct or equal). Returns RG_ERR_UNSUPPORTED, having done
+ * nothing, when the last axis has no compile-time kernel (n2 odd, n2 / 2 not a power of two in
+ * the instantiated range): the caller then makes the two calls. */
+int rocketgpu_poisson_dct2_eigdiv(const float *in, float *out, int64_t n0, int64_t n1, int64_t n2, const float *lam,
+                                  void *stream);
 int rocketgpu_poisson_update(double *u, float *u_lo, const float *delta, int64_t total, void *stream);
 int rocketgpu_poisson_residual(const double *u, const float *u_lo, const double *f, float *r32, int64_t n0,
                                int64_t n1, int64_t n2, double *sumsq, void *stream);

@@ -84,6 +84,19 @@ enum Op : int {
 };
 
 constexpr int kFlagStream = 4;
+// OP_DCT2_HALF row walk over the last axis of a C-contiguous n0 x n1 x n2 volume: divide every
+// output by the Neumann eigenvalue lam0[k0] + lam1[k1] + lam2[k2] (aux3 = lam0 | lam1 | lam2,
+// aux_s = n0, aux_n = n1; the (0, 0, 0) output set to 0) -- the Poisson solver's spectral divide
+// fused into its DCT-II
+constexpr int kFlagEigDiv = 8;
+// The divide of the Poisson spectral step (the float32 preconditioner of an exact fixed-point
+// refinement): in float32 the fast division (two ulp; an IEEE division per point cost the fused
+// DCT-II pass 60 % more time), in float64 the IEEE one. The separate divide kernel uses the same
+// function, so both routes give the same bits.
+template <typename T> __device__ __forceinline__ T eig_div(T y, T lam) {
+  if constexpr (sizeof(T) == 4) return __fdividef(y, lam);
+  else return y / lam;
+}
 
 // L2 cache policy for a launch's input loads: evict-first when the launch reads its input once
 // (kFlagStream), so that it does not push out of L2 the data the next launch reads; evict-normal
@@ -140,6 +153,7 @@ struct KArgs {
   const void *aux2;  // op-specific second table (Bluestein spectrum, ...)
   int aux_n;         // op-specific integer (four-step: number of columns)
   int aux_s;         // op-specific integer (four-step: low-table split shift)
+  const void *aux3;  // op-specific third table (kFlagEigDiv: the eigenvalues)
   FFTCore core;
 };
 

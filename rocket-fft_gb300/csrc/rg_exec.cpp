@@ -382,6 +382,7 @@ void run_job(const Job &j, cudaStream_t st) {
   a.fct = j.fct;
   a.aux = j.aux;
   a.aux2 = j.aux2;
+  a.aux3 = j.aux3;
   a.aux_n = j.aux_n;
   a.aux_s = j.aux_s;
   a.bscale = j.bscale;

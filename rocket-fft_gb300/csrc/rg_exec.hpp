@@ -38,6 +38,12 @@ void exec_c2c_sym(DType dt, const NdArray &in, const NdArray &out, const Axes &a
 // Real-to-real transforms (rg_r2r.cu): DCT (cosine) / DST types 1-4, FFTPACK r2r, Hartley.
 // adjoint: the transpose of the transform (DCT/DST-II <-> III with the element-0 weight of the
 // transpose; types 1 and 4 are symmetric).
+// DCT-II of a C-contiguous float32 n0 x n1 x n2 volume over its three axes (fct 1) whose last
+// pass divides by the Neumann eigenvalues lam = lam0 | lam1 | lam2 as it stores (0 at the origin):
+// the Poisson solver's DCT-II and eigenvalue divide in one. False (nothing done) when the last
+// axis has no compile-time kernel.
+bool dct2_eigdiv_3d(const float *in, float *out, int64_t n0, int64_t n1, int64_t n2, const float *lam,
+                    cudaStream_t st);
 void exec_dcst(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, int type, bool cosine,
                double fct, bool ortho, cudaStream_t st, bool adjoint = false);
 void exec_r2r_fftpack(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, bool real2hermitian,

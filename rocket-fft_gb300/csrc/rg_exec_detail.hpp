@@ -40,7 +40,7 @@ struct Job {
   int64_t nrows;
   bool cin, cout;
   double fct;
-  const void *aux = nullptr, *aux2 = nullptr;
+  const void *aux = nullptr, *aux2 = nullptr, *aux3 = nullptr;
   int aux_n = 1, aux_s = 0;
   double bscale = 1.0;  // interior half-spectrum bin scale (r2c/c2r adjoints)
   double e0 = 1.0;      // fused DCT ops: element-0 weight

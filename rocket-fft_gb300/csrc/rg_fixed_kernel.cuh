@@ -673,9 +673,24 @@ __global__ void __launch_bounds__(FxCfg<T, OP, E, COL>::NT, FxCfg<T, OP, E, COL>
       if (sr < rows) {
         T *p = reinterpret_cast<T *>(a.out) + side_offset32(a.st, row0 + uint32_t(sr));
         const cx<T> *row = buf + sr * PITCH;
+        // kFlagEigDiv: row g = k0 n1 + k1; the same float operations as the separate divide
+        const bool eig = (a.flags & kFlagEigDiv) != 0;
+        const T *lam2 = nullptr;
+        T lam01 = T(0);
+        bool origin = false;
+        if (eig) {
+          const T *lam = reinterpret_cast<const T *>(a.aux3);
+          const uint32_t g = row0 + uint32_t(sr), n1 = uint32_t(a.aux_n);
+          const uint32_t k0 = g / n1, k1 = g - k0 * n1;
+          lam01 = lam[k0] + lam[a.aux_s + k1];
+          lam2 = lam + a.aux_s + n1;
+          origin = g == 0;
+        }
         auto put = [&](int kk, T y) {
           const int pos = sine ? N - 1 - kk : kk;
-          p[pos * so] = pos == 0 ? y * e0 : y;
+          y = pos == 0 ? y * e0 : y;
+          if (eig) y = (origin && pos == 0) ? T(0) : eig_div<T>(y, lam01 + lam2[pos]);
+          p[pos * so] = y;
         };
         auto emit = [&](int k, cx<T> X) {  // 0 < k < L
           const cx<T> z = mul<T>(__ldg(t2 + k), X);

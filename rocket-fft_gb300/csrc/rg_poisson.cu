@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/rocket_gpu.h"
+#include "rg_common.cuh"
 #include "rg_error.hpp"
 #include "rg_exec.hpp"
 #include "rg_launch.hpp"
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(256, 4) eigdiv_kernel(T *X, Grid g, const T *l
           if (base[u]) x[u] = base[u][k2];
 #pragma unroll
         for (int u = 0; u < ROWS; ++u)
-          if (base[u]) base[u][k2] = (base[u] == X && k2 == 0) ? T(0) : x[u] / (lam01[u] + l2k[0]);
+          if (base[u]) base[u][k2] = (base[u] == X && k2 == 0) ? T(0) : rg::eig_div<T>(x[u], lam01[u] + l2k[0]);
       } else {
         using VT = typename Vec<T, V>::type;
         VT x[ROWS];
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(256, 4) eigdiv_kernel(T *X, Grid g, const T *l
           if (base[u]) {
             T *e = reinterpret_cast<T *>(&x[u]);
 #pragma unroll
-            for (int v = 0; v < V; ++v) e[v] = e[v] / (lam01[u] + l2k[v]);
+            for (int v = 0; v < V; ++v) e[v] = rg::eig_div<T>(e[v], lam01[u] + l2k[v]);
             if (base[u] == X && k2 == 0) e[0] = T(0);
             *reinterpret_cast<VT *>(base[u] + k2) = x[u];
           }
@@ -683,6 +684,17 @@ extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_eigdiv(v
     });
     rg::note_launch();
     RG_CUDA(cudaGetLastError());
+  });
+}
+
+extern "C" __attribute__((visibility("default"))) int rocketgpu_poisson_dct2_eigdiv(const float *in, float *out,
+                                                                                   int64_t n0, int64_t n1,
+                                                                                   int64_t n2, const float *lam,
+                                                                                   void *stream) {
+  return guarded([&] {
+    RG_CHECK(n0 > 0 && n1 > 0 && n2 > 0, RG_ERR_ARG, "empty grid");
+    RG_CHECK(rg::dct2_eigdiv_3d(in, out, n0, n1, n2, lam, static_cast<cudaStream_t>(stream)), RG_ERR_UNSUPPORTED,
+             "no compile-time DCT-II kernel for the last axis");
   });
 }
 

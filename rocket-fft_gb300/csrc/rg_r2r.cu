@@ -371,6 +371,46 @@ template <typename T> __global__ void __launch_bounds__(256) hartley_gen_kernel(
 
 }  // namespace
 
+bool dct2_eigdiv_3d(const float *in, float *out, int64_t n0, int64_t n1, int64_t n2, const float *lam,
+                    cudaStream_t st) {
+  NdArray a, b;
+  a.data = const_cast<float *>(in);
+  b.data = out;
+  a.shape = b.shape = {n0, n1, n2};
+  a.stride = b.stride = {n1 * n2, n2, 1};
+  const Axes axes = {0, 1, 2};
+  // the last axis' job, checked before any work: it must run in the compile-time kernel
+  const detail::Batch bl = detail::make_batch(b.shape, b.stride, b.stride, 2);
+  detail::Job j{};
+  j.dt = DType::F32;
+  j.op = OP_DCT2_HALF;
+  j.n = j.nin = j.nout = int(n2);
+  j.L = int(n2 / 2);
+  j.Lsm = j.L + 1;
+  j.in = out;
+  j.out = out;
+  j.ld = detail::make_side(1, bl.shape, bl.s_in);
+  j.st = detail::make_side(1, bl.shape, bl.s_out);
+  j.nrows = bl.nrows;
+  j.fct = 1.0;
+  j.e0 = 1.0;
+  j.flags = kFlagEigDiv;
+  j.aux_n = int(n1);
+  j.aux_s = int(n0);
+  j.aux3 = lam;
+  if (n2 % 2 != 0 || !fused_enabled() || n0 * n1 >= (int64_t(1) << 31) || bl.nrows != n0 * n1 ||
+      !detail::fixed_job_ok(j))
+    return false;
+  j.aux = get_roots(uint64_t(4 * n2), uint64_t(n2), DType::F32);
+  j.aux2 = get_roots(uint64_t(n2), uint64_t(n2 / 4 + 1), DType::F32);
+  real_nd(a, b, {0, 1}, 1.0, [&](int64_t n, const void *src, const Side &ld, void *dst, const Side &sd, int64_t rows,
+                                 double f) {
+    r2r_axis(DType::F32, K_DCT2, n, src, ld, dst, sd, rows, true, false, f, 1.0, 1.0, st);
+  });
+  detail::run_job(j, st);
+  return true;
+}
+
 void exec_dcst(DType dt, const NdArray &in, const NdArray &out, const Axes &axes, int type, bool cosine,
                double fct, bool ortho, cudaStream_t st, bool adjoint) {
   const double r2 = 1.4142135623730951, h2 = 0.7071067811865476;

@@ -34,6 +34,7 @@ from . import _lib
 from . import pocketfft as _pf
 
 AXES = np.array([0, 1, 2], dtype=np.int64)
+_UNSUPPORTED = 2  # RG_ERR_UNSUPPORTED (include/rocket_gpu.h): a valid request this build does not implement
 
 
 def _bind():
@@ -64,6 +65,8 @@ def _bind():
         lib.rocketgpu_poisson_init_fx.restype = ctypes.c_int
         lib.rocketgpu_poisson_prepare.argtypes = [P, P, i64, P, P]
         lib.rocketgpu_poisson_prepare.restype = ctypes.c_int
+        lib.rocketgpu_poisson_dct2_eigdiv.argtypes = [P, P, i64, i64, i64, P, P]
+        lib.rocketgpu_poisson_dct2_eigdiv.restype = ctypes.c_int
         lib._poisson_bound = True
     return lib
 
@@ -98,14 +101,24 @@ class NeumannPoisson:
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
 
-    def spectral_solve(self, rhs, out=None, work=None):
-        """out = A^{-1} rhs through DCT-II, eigenvalue divide, DCT-III (rhs's precision)."""
+    def spectral_solve(self, rhs, out=None, work=None, fused=True):
+        """out = A^{-1} rhs through DCT-II, eigenvalue divide, DCT-III (rhs's precision). For
+        float32 the divide runs inside the DCT-II's last pass where a compile-time kernel exists
+        (the same results; ``fused=False`` makes the separate calls)."""
         work = torch.empty_like(rhs) if work is None else work
         out = torch.empty_like(rhs) if out is None else out
-        _pf.dct(rhs, work, AXES, 2, 1.0, False, 1)
-        _check(self.lib, self.lib.rocketgpu_poisson_eigdiv(work.data_ptr(), rhs.element_size(), *self.shape,
-                                                            (self.lam32 if rhs.element_size() == 4 else self.lam).data_ptr(),
-                                                            self._stream()))
+        done = False
+        if fused and rhs.dtype == torch.float32 and rhs.is_contiguous() and work.is_contiguous():
+            st = self.lib.rocketgpu_poisson_dct2_eigdiv(rhs.data_ptr(), work.data_ptr(), *self.shape,
+                                                        self.lam32.data_ptr(), self._stream())
+            done = st == 0
+            if st != 0 and st != _UNSUPPORTED:
+                _check(self.lib, st)
+        if not done:
+            _pf.dct(rhs, work, AXES, 2, 1.0, False, 1)
+            _check(self.lib, self.lib.rocketgpu_poisson_eigdiv(work.data_ptr(), rhs.element_size(), *self.shape,
+                                                                (self.lam32 if rhs.element_size() == 4 else self.lam).data_ptr(),
+                                                                self._stream()))
         _pf.dct(work, out, AXES, 3, self.fct, False, 1)
         return out
 

@@ -131,3 +131,24 @@ def test_fixed_point_residual_exact(rg, cuda, shape):
     got = r32.cpu().numpy().astype(np.float64)
     assert np.abs(got - want).max() <= 1e-6 * np.abs(want).max()
     assert abs(float(ss.item()) - float(np.sum(want * want))) <= 1e-5 * float(np.sum(want * want))
+
+
+@pytest.mark.parametrize("shape", [(16, 24, 128), (8, 12, 256), (32, 32, 32), (24, 20, 18)])
+def test_dct2_eigdiv_fused_matches(rg, cuda, shape):
+    """The DCT-II with the eigenvalue divide in its last pass (rocketgpu_poisson_dct2_eigdiv)
+    gives the same float32 spectrum, bit for bit, as the DCT-II followed by the separate divide;
+    where the last axis has no compile-time half-length kernel (n2 = 32, 18) the entry point
+    declines and the solver makes the two calls."""
+    torch = cuda
+    P = importlib.import_module("rocket_fft_gb300.poisson")
+    S = P.NeumannPoisson(shape)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    r = torch.randn(shape, dtype=torch.float32, device="cuda", generator=g)
+    a, b = torch.empty_like(r), torch.empty_like(r)
+    w1, w2 = torch.empty_like(r), torch.empty_like(r)
+    S.spectral_solve(r, out=a, work=w1, fused=True)
+    S.spectral_solve(r, out=b, work=w2, fused=False)
+    torch.cuda.synchronize()
+    assert torch.equal(w1, w2) and torch.equal(a, b)
+    st = S.lib.rocketgpu_poisson_dct2_eigdiv(r.data_ptr(), w1.data_ptr(), *shape, S.lam32.data_ptr(), S._stream())
+    assert st == (0 if shape[2] in (128, 256) else P._UNSUPPORTED)
