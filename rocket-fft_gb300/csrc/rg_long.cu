@@ -138,13 +138,8 @@ void run_long(int64_t m, const void *in, const Side &ld, void *out, const Side &
   a.conj_out = cout ? 1 : 0;
   a.fct = float(fct);
   // pass twiddles of each phase's schedule (rg_long.cuh, lg::radix)
-  if (lg::first_radix(s.e1, s.e2) == 32) {
-    a.twA = get_pass_tw(1 << s.e1, 32, dt);
-    a.twB = get_pass_tw(1 << s.e2, 32, dt);
-  } else {
-    a.twA = get_core(1 << s.e1, dt).core.tw;
-    a.twB = get_core(1 << s.e2, dt).core.tw;
-  }
+  a.twA = lg::first_radix(KIND, s.e1, s.e2, true) == 32 ? get_pass_tw(1 << s.e1, 32, dt) : get_core(1 << s.e1, dt).core.tw;
+  a.twB = lg::first_radix(KIND, s.e1, s.e2, false) == 32 ? get_pass_tw(1 << s.e2, 32, dt) : get_core(1 << s.e2, dt).core.tw;
   const SplitTables sp = get_split(uint64_t(m), dt);
   a.lo = sp.lo;
   a.hi = sp.hi;

@@ -13,8 +13,9 @@
 // A phase-A tile is C = TT / n1 adjacent columns of one transform (its HBM reads are C-element
 // segments: lanes run across the columns first); a phase-B tile is D = TT / n2 adjacent rows of
 // Y (its HBM writes are D-element segments). Each thread runs one first-pass butterfly (radix
-// 16, at most 64 registers, TT / 16 threads; radix 32 when both phases are 2^9 or 2^10 points,
-// at most 128 registers, TT / 32 threads) and the later passes' butterflies in turn. Both phases
+// 16, at most 64 registers, TT / 16 threads; radix 32 for phases of 2^9 or 2^10 points, at most
+// 128 registers, TT / 32 threads, where a radix-16 first pass of the other phase of a complex
+// transform takes two butterflies per thread) and the later passes' butterflies in turn. Both phases
 // read their first radix pass straight from global memory into registers and write their last
 // pass straight back; the passes in between run in place in one shared buffer, whose line pitch
 // and padding period are chosen at compile time to minimise shared-memory wavefronts over the
@@ -169,16 +170,23 @@ constexpr int radix(int E, int r0, int p) { return r0 == 32 ? (p == 0 ? 32 : (1 
 constexpr int ns(int E, int r0, int p) { return r0 == 32 ? (p == 0 ? 1 : 32) : fx::ns_of(E, p); }
 // offset of pass p's twiddles in the phase's table (r0 = 32: the table of get_pass_tw)
 constexpr int twoff(int E, int r0, int p) { return r0 == 32 ? 0 : fx::tw_of(E, p); }
-// First-pass radix of a shape: 32 when both phase lengths are 2^RG_LONG_R32_MIN .. 2^10, else
-// 16. For 2^9 and 2^10 the 32 x 2^(E-5) schedule has two passes instead of three (one
-// shared-memory round trip and two barriers fewer per tile): measured on GB300, c2c 2^18 .. 2^20
+// First-pass radix of a phase of 2^E points: 32 for 2^RG_LONG_R32_MIN .. 2^10, else 16. For 2^9
+// and 2^10 the 32 x 2^(E-5) schedule has two passes instead of three (one shared-memory round
+// trip and two barriers fewer per tile): measured on GB300 with both phases so, c2c 2^18 .. 2^20
 // +11 %, r2c 2^21 +6 %. Taking 2^8 phases as 32 x 8 too (same pass count) measured -3 to -8 %
-// except c2c 2^17 (+4 %), so the default range starts at 2^9.
+// except c2c 2^17 (+4 %), so the default range starts at 2^9. A CTA whose phases take radix 32
+// and 16 runs TT / 32 threads; its radix-16 first pass then takes two butterflies per thread.
 #ifndef RG_LONG_R32_MIN
 #define RG_LONG_R32_MIN 9
 #endif
-constexpr int first_radix(int E1, int E2) {
-  return E1 >= RG_LONG_R32_MIN && E1 <= 10 && E2 >= RG_LONG_R32_MIN && E2 <= 10 ? 32 : 16;
+constexpr int phase_radix(int E) { return E >= RG_LONG_R32_MIN && E <= 10 ? 32 : 16; }
+// The first-pass radix of phase A (phase_a) or B of a shape of kind `kind`. Where only one phase
+// takes radix 32 (2^8 x 2^9, 2^10 x 2^11), the complex transforms mix the two (c2c 2^17 +2.5 %,
+// 2^21 +7 %) and the real ones keep radix 16 in both (mixed, r2c 2^18 measured 6 % slower).
+constexpr int first_radix(int kind, int E1, int E2, bool phase_a) {
+  const int ra = phase_radix(E1), rb = phase_radix(E2);
+  if (ra != rb && kind != LG_C2C) return 16;
+  return phase_a ? ra : rb;
 }
 
 constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, int r0) {
@@ -187,14 +195,15 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
   for (int w = 0; w < NT / 32 && w < 4; ++w) {
     int slot[32] = {};
     // first pass (radix r0, output position r0 j + k)
-    for (int k = 0; k < r0; ++k) {
-      for (int l = 0; l < 32; ++l) {
-        const int u = 32 * w + l;
-        const int line = a_side ? u % M : u / (L / r0), j = a_side ? u / M : u % (L / r0);
-        slot[l] = line * pitch + spad(r0 * j + k, ps);
+    for (int it = 0; it < (M * (L / r0)) / NT; ++it)
+      for (int k = 0; k < r0; ++k) {
+        for (int l = 0; l < 32; ++l) {
+          const int u = 32 * w + l + it * NT;
+          const int line = a_side ? u % M : u / (L / r0), j = a_side ? u / M : u % (L / r0);
+          slot[l] = line * pitch + spad(r0 * j + k, ps);
+        }
+        total += wave(slot);
       }
-      total += wave(slot);
-    }
     for (int p = 1; p < NP; ++p) {
       const int R = radix(E, r0, p), LR = L / R, NS = ns(E, r0, p);
       for (int it = 0; it < (M * LR) / NT; ++it)
@@ -243,35 +252,37 @@ constexpr int pick_layout(int c5, int c4, int c3) {
 }
 }  // namespace lg
 
-// Compile-time geometry: n1 = 2^E1 (phase-A length), n2 = 2^E2, tile of TT = 2^ET elements.
-template <int E1, int E2, int ET> struct LgCfg {
+// Compile-time geometry of kind KIND: n1 = 2^E1 (phase-A length), n2 = 2^E2, tile of TT = 2^ET
+// elements.
+template <int E1, int E2, int ET, int KIND> struct LgCfg {
   static constexpr int N1 = 1 << E1, N2 = 1 << E2, TT = 1 << ET;
   static constexpr int C = TT / N1, D = TT / N2;  // columns per A tile, rows per B tile
-  static constexpr int R0 = lg::first_radix(E1, E2);
-  static constexpr int NT = TT / R0;              // threads: one first-pass butterfly each
+  static constexpr int R0A = lg::first_radix(KIND, E1, E2, true), R0B = lg::first_radix(KIND, E1, E2, false);
+  static constexpr int RMAX = R0A > R0B ? R0A : R0B;
+  static constexpr int NT = TT / RMAX;            // threads: one radix-RMAX butterfly each
   // CTAs per SM the registers are sized for: 64 registers a thread at 16 points per thread, 128
   // at 32
-  static constexpr int MINB = R0 == 32 ? 512 / NT : 1024 / NT;
+  static constexpr int MINB = RMAX == 32 ? 512 / NT : 1024 / NT;
   // shared layout of each phase: padding period and line pitch (each candidate period searched
   // in a constant of its own, within the compiler's constant-evaluation budget)
-  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5, R0), A4 = lg::best_pitch(E1, C, NT, true, 4, R0);
-  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3, R0);
-  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5, R0), B4 = lg::best_pitch(E2, D, NT, false, 4, R0);
-  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3, R0);
+  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5, R0A), A4 = lg::best_pitch(E1, C, NT, true, 4, R0A);
+  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3, R0A);
+  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5, R0B), B4 = lg::best_pitch(E2, D, NT, false, 4, R0B);
+  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3, R0B);
   static constexpr int LA = lg::pick_layout(A5, A4, A3), LB = lg::pick_layout(B5, B4, B3);
   static constexpr int PA = LA & 0xffff, PB = LB & 0xffff;  // line pitches (slots)
   static constexpr int SA = LA >> 16, SB = LB >> 16;        // padding periods (log2)
   static constexpr int SLOTS = C * PA > D * PB ? C * PA : D * PB;
   // radix of phase A's last pass, and its per-tile factors W_n^{col k NS} (k = 1 .. RA-1, one
   // per column of the tile)
-  static constexpr int RA = lg::radix(E1, R0, lg::np(E1, R0) - 1);
+  static constexpr int RA = lg::radix(E1, R0A, lg::np(E1, R0A) - 1);
   static constexpr int FTAB = (RA - 1) * C;
   // the tile, the factor table, then two control words (ticket, wait failure): no static
   // shared memory, so the dynamic size may be raised to the device's opt-in maximum
   static constexpr size_t CTRL = size_t(SLOTS + FTAB) * 8;
   static constexpr size_t SMEM = CTRL + 16;
   static_assert(C >= 2 && D >= 2 && C <= 32 && D <= 32, "tile shape");
-  static_assert(lg::radix(E1, R0, 0) == R0 && lg::radix(E2, R0, 0) == R0, "first pass radix");
+  static_assert(lg::radix(E1, R0A, 0) == R0A && lg::radix(E2, R0B, 0) == R0B, "first pass radix");
 };
 
 // ---- passes over lines of length 2^E held in shared memory (line l at sm + l * PITCH) ----
@@ -383,7 +394,7 @@ __device__ __forceinline__ void pair_unit(int t, int i, int q, int &la, int &pa,
 template <int KIND, int E1, int E2, int ET>
 __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const float2 *__restrict__ x,
                                            float2 *__restrict__ y, int part) {
-  using Cf = LgCfg<E1, E2, ET>;
+  using Cf = LgCfg<E1, E2, ET, KIND>;
   constexpr int N1 = Cf::N1, N2 = Cf::N2, C = Cf::C, NT = Cf::NT, PA = Cf::PA, SA = Cf::SA;
   const float2 *tw = reinterpret_cast<const float2 *>(a.twA);
   const float2 *lo = reinterpret_cast<const float2 *>(a.lo), *hi = reinterpret_cast<const float2 *>(a.hi);
@@ -402,27 +413,36 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     }
   }
   if constexpr (KIND != LG_C2R) {
-    // first pass: radix R0 straight from global memory; lanes run across the C columns first
-    constexpr int R = Cf::R0, LR = N1 / R, UNITS = C * LR;
-    static_assert(UNITS == NT, "one unit per thread");
-    const int u = int(threadIdx.x);
-    const int c = u % C, j = u / C;
+    // first pass: radix R0A straight from global memory (IT butterflies per thread, all loads
+    // first); lanes run across the C columns first
+    constexpr int R = Cf::R0A, LR = N1 / R, UNITS = C * LR, IT = UNITS / NT;
+    static_assert(UNITS % NT == 0, "whole first-pass units per thread");
     const uint64_t pol = input_policy(true);
-    const float2 *p = x + part * C + int64_t(j) * N2 + c;
     constexpr int64_t STEP = int64_t(LR) * N2;
-    float2 v[R];
+    float2 v[IT][R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = ld_in(p + k * STEP, pol);
-    if (a.conj_in) {
+    for (int it = 0; it < IT; ++it) {
+      const int u = int(threadIdx.x) + it * NT;
+      const int c = u % C, j = u / C;
+      const float2 *p = x + part * C + int64_t(j) * N2 + c;
 #pragma unroll
-      for (int k = 0; k < R; ++k) v[k].y = -v[k].y;
+      for (int k = 0; k < R; ++k) v[it][k] = ld_in(p + k * STEP, pol);
     }
-    dft<float, R>(v);
-    float2 *l0 = sm + c * PA;
 #pragma unroll
-    for (int k = 0; k < R; ++k) l0[lg::sp_k<1, SA>(j * R, k)] = v[k];
+    for (int it = 0; it < IT; ++it) {
+      const int u = int(threadIdx.x) + it * NT;
+      const int c = u % C, j = u / C;
+      if (a.conj_in) {
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[it][k].y = -v[it][k].y;
+      }
+      dft<float, R>(v[it]);
+      float2 *l0 = sm + c * PA;
+#pragma unroll
+      for (int k = 0; k < R; ++k) l0[lg::sp_k<1, SA>(j * R, k)] = v[it][k];
+    }
     __syncthreads();
-    lg_middles<E1, Cf::R0, C, NT, PA, SA, 1, lg::np(E1, Cf::R0) - 1>(sm, tw);
+    lg_middles<E1, Cf::R0A, C, NT, PA, SA, 1, lg::np(E1, Cf::R0A) - 1>(sm, tw);
   } else {
     // c2r: merge the half spectrum X (m + 1 elements, m = n1 n2) of columns j2 and n2 - j2
     // into conj(Z) on chip, then every pass but the last in shared memory
@@ -458,12 +478,12 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     }
     if (t == 0 && threadIdx.x == 0) merge(0, N1 / 2, 0, N1 / 2, M / 2, false);
     __syncthreads();
-    lg_middles<E1, Cf::R0, C, NT, PA, SA, 0, lg::np(E1, Cf::R0) - 1>(sm, tw);
+    lg_middles<E1, Cf::R0A, C, NT, PA, SA, 0, lg::np(E1, Cf::R0A) - 1>(sm, tw);
   }
   // last pass: outputs k1 = j + k * NS, times W_n^{j2 k1}, to Y[k1][j2]; lanes across the C
   // columns first (L2-resident stores, kept there with an evict-last policy)
   {
-    constexpr int P = lg::np(E1, Cf::R0) - 1, R = lg::radix(E1, Cf::R0, P), LR = N1 / R, NS = LR;
+    constexpr int P = lg::np(E1, Cf::R0A) - 1, R = lg::radix(E1, Cf::R0A, P), LR = N1 / R, NS = LR;
     constexpr int UNITS = C * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
     static_assert(R == Cf::RA, "factor table radix");
@@ -473,7 +493,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       const int u = int(threadIdx.x) + it * NT;
       const int c = u % C, j = u / C;
       float2 v[R];
-      lg_last_one<E1, Cf::R0, PA, SA>(sm, tw, c, j, v);
+      lg_last_one<E1, Cf::R0A, PA, SA>(sm, tw, c, j, v);
       const int col = KIND == LG_C2R ? pair_index<N2, C>(part, c) : part * C + c;
       float2 *yc = y + col;
       const float2 wj = split_twiddle<float>(lo, hi, a.shift, uint32_t(col) * uint32_t(j));
@@ -492,7 +512,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
 template <int KIND, int E1, int E2, int ET>
 __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const float2 *__restrict__ yg,
                                            float2 *__restrict__ X, int part) {
-  using Cf = LgCfg<E1, E2, ET>;
+  using Cf = LgCfg<E1, E2, ET, KIND>;
   constexpr int N1 = Cf::N1, N2 = Cf::N2, D = Cf::D, NT = Cf::NT, PB = Cf::PB, SB = Cf::SB;
   const float2 *tw = reinterpret_cast<const float2 *>(a.twB);
   // row of Y held by line r
@@ -500,20 +520,29 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     const int k1 = KIND == LG_R2C ? pair_index<N1, D>(part, r) : part * D + r;
     return yg + int64_t(k1) * N2;
   };
-  // first pass: radix R0 from Y (L2); lanes along the row
+  // first pass: radix R0B from Y (L2; IT butterflies per thread, all loads first); lanes along
+  // the row
   {
-    constexpr int R = Cf::R0, LR = N2 / R, UNITS = D * LR;
-    static_assert(UNITS == NT, "one unit per thread");
-    const int u = int(threadIdx.x);
-    const int r = u / LR, j = u % LR;
-    const float2 *p = yrow(r) + j;
-    float2 v[R];
+    constexpr int R = Cf::R0B, LR = N2 / R, UNITS = D * LR, IT = UNITS / NT;
+    static_assert(UNITS % NT == 0, "whole first-pass units per thread");
+    float2 v[IT][R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = __ldcg(p + k * LR);
-    dft<float, R>(v);
-    float2 *l = sm + r * PB;
+    for (int it = 0; it < IT; ++it) {
+      const int u = int(threadIdx.x) + it * NT;
+      const int r = u / LR, j = u % LR;
+      const float2 *p = yrow(r) + j;
 #pragma unroll
-    for (int k = 0; k < R; ++k) l[lg::sp_k<1, SB>(j * R, k)] = v[k];
+      for (int k = 0; k < R; ++k) v[it][k] = __ldcg(p + k * LR);
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int u = int(threadIdx.x) + it * NT;
+      const int r = u / LR, j = u % LR;
+      dft<float, R>(v[it]);
+      float2 *l = sm + r * PB;
+#pragma unroll
+      for (int k = 0; k < R; ++k) l[lg::sp_k<1, SB>(j * R, k)] = v[it][k];
+    }
   }
   __syncthreads();
   if (a.flags & kLongDiscard) {
@@ -526,9 +555,9 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
   const float sgn = a.conj_out ? -fct : fct;
   const uint64_t pol = input_policy((a.flags & kLongEvictOut) != 0);
   if constexpr (KIND != LG_R2C) {
-    lg_middles<E2, Cf::R0, D, NT, PB, SB, 1, lg::np(E2, Cf::R0) - 1>(sm, tw);
+    lg_middles<E2, Cf::R0B, D, NT, PB, SB, 1, lg::np(E2, Cf::R0B) - 1>(sm, tw);
     // last pass: outputs k2 = j + k * NS of row r to X[r + k2 n1]; lanes across the D rows first
-    constexpr int P = lg::np(E2, Cf::R0) - 1, R = lg::radix(E2, Cf::R0, P), LR = N2 / R, NS = LR;
+    constexpr int P = lg::np(E2, Cf::R0B) - 1, R = lg::radix(E2, Cf::R0B, P), LR = N2 / R, NS = LR;
     constexpr int UNITS = D * LR, ITER = UNITS / NT;
     static_assert(UNITS % NT == 0, "whole iterations");
     float2 *Xt = X + part * D;
@@ -537,7 +566,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
       const int u = int(threadIdx.x) + it * NT;
       const int r = u % D, j = u / D;
       float2 v[R];
-      lg_last_one<E2, Cf::R0, PB, SB>(sm, tw, r, j, v);
+      lg_last_one<E2, Cf::R0B, PB, SB>(sm, tw, r, j, v);
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const int64_t k2 = j + k * NS;
@@ -546,7 +575,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
     }
   } else {
     // r2c: every pass on chip, then the split of each row pair into X_k and X_{m-k}
-    lg_middles<E2, Cf::R0, D, NT, PB, SB, 1, lg::np(E2, Cf::R0)>(sm, tw);
+    lg_middles<E2, Cf::R0B, D, NT, PB, SB, 1, lg::np(E2, Cf::R0B)>(sm, tw);
     constexpr int64_t M = int64_t(N1) * N2;
     constexpr int H = D / 2;
     const float2 *lo2 = reinterpret_cast<const float2 *>(a.lo2), *hi2 = reinterpret_cast<const float2 *>(a.hi2);
@@ -598,9 +627,9 @@ __device__ __forceinline__ void red_release_add(int *p, int v) {
 // KIND: LG_C2C (complex in, complex out), LG_R2C (real in, n/2+1 complex out), LG_C2R. Row
 // offsets from the sides are in units of the side's element (float for real rows).
 template <int KIND, int E1, int E2, int ET>
-__global__ void __launch_bounds__(LgCfg<E1, E2, ET>::NT, LgCfg<E1, E2, ET>::MINB)
+__global__ void __launch_bounds__(LgCfg<E1, E2, ET, KIND>::NT, LgCfg<E1, E2, ET, KIND>::MINB)
     long_kernel(const __grid_constant__ LongArgs a) {
-  using Cf = LgCfg<E1, E2, ET>;
+  using Cf = LgCfg<E1, E2, ET, KIND>;
   constexpr int64_t n = int64_t(1) << (E1 + E2);
   constexpr int TPA = Cf::N2 / Cf::C;  // A tiles per transform
   constexpr int TPB = Cf::N1 / Cf::D;  // B tiles per transform

@@ -12,7 +12,7 @@ namespace rg {
 
 template <int KIND, int E1, int E2, int ET>
 void launch_long(LongArgs &a, int64_t tickets, cudaStream_t st) {
-  using Cf = LgCfg<E1, E2, ET>;
+  using Cf = LgCfg<E1, E2, ET, KIND>;
   const void *fn = reinterpret_cast<const void *>(&long_kernel<KIND, E1, E2, ET>);
   set_smem_attr(fn, Cf::SMEM);
   const int64_t res = resident_ctas(fn, Cf::NT, Cf::SMEM);
