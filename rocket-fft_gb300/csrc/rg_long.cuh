@@ -42,8 +42,10 @@
 // - i W_n^k (Z_k - conj Z_{m-k}) / 2 needs Z_k and Z_{m-k} together: with k = k1 + n1 k2,
 // m - k = (n1 - k1) + n1 (n2 - 1 - k2), so an r2c phase-B tile holds D/2 rows k1 and their
 // mirror rows n1 - k1 (tile 0: rows 0 and n1/2, which mirror onto themselves, and rows
-// 1 .. D/2-1 with their mirrors), runs every pass on chip and stores X_k and X_{m-k} from each
-// pair. c2r is the mirror image: its phase-A tile holds columns j2 and n2 - j2, merges the
+// 1 .. D/2-1 with their mirrors) and stores X_k and X_{m-k} from each pair: past tile 0 the last
+// pass runs a row's butterfly and the mirror row's mirrored butterfly in lanes l and l + 16 of
+// one warp, which exchange their halves by shuffle; tile 0 splits from shared memory. c2r is
+// the mirror image: its phase-A tile holds columns j2 and n2 - j2, merges the
 // Hermitian half spectrum into conj(Z) as it loads, and phase B stores conj of the result as
 // the real pairs.
 #pragma once
@@ -189,7 +191,9 @@ constexpr int first_radix(int kind, int E1, int E2, bool phase_a) {
   return phase_a ? ra : rb;
 }
 
-constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, int r0) {
+// pair_last: the last pass of the r2c phase B instead (lg_phase_b): lane l < 16 of a warp on
+// primary line i at butterfly j, lane l + 16 on the mirror line M-1-i at butterfly NS-1-j.
+constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, int r0, bool pair_last) {
   const int L = 1 << E, NP = np(E, r0);
   int total = 0;
   for (int w = 0; w < NT / 32 && w < 4; ++w) {
@@ -211,7 +215,12 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
           for (int l = 0; l < 32; ++l) {  // reads
             const int u = 32 * w + l + it * NT;
             const bool last = p == NP - 1;
-            const int line = last ? u % M : u / LR, j = last ? u / M : u % LR;
+            int line = last ? u % M : u / LR, j = last ? u / M : u % LR;
+            if (last && pair_last) {
+              const int v = (w + it * (NT / 32)) * 16 + (l & 15), i = v % (M / 2), jj = v / (M / 2);
+              line = l >= 16 ? M - 1 - i : i;
+              j = l >= 16 ? NS - 1 - jj : jj;
+            }
             slot[l] = line * pitch + spad(j + k * LR, ps);
           }
           total += wave(slot);
@@ -230,11 +239,11 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
 }
 // For padding period 2^ps: the pitch (>= the padded line length, within 16 slots of it) with
 // the fewest wavefronts, as cost * 2^16 + pitch.
-constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps, int r0) {
+constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps, int r0, bool pair_last = false) {
   const int base = spad((1 << E) - 1, ps) + 1;
   int best = base, cost = 1 << 14;
   for (int p = base; p < base + 16; ++p) {
-    const int c = phase_waves(E, M, NT, p, a_side, ps, r0);
+    const int c = phase_waves(E, M, NT, p, a_side, ps, r0, pair_last);
     if (c < cost) {
       cost = c;
       best = p;
@@ -267,8 +276,10 @@ template <int E1, int E2, int ET, int KIND> struct LgCfg {
   // in a constant of its own, within the compiler's constant-evaluation budget)
   static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5, R0A), A4 = lg::best_pitch(E1, C, NT, true, 4, R0A);
   static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3, R0A);
-  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5, R0B), B4 = lg::best_pitch(E2, D, NT, false, 4, R0B);
-  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3, R0B);
+  static constexpr bool PAIRB = KIND == LG_R2C;  // r2c: phase B's last pass on line pairs
+  static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5, R0B, PAIRB);
+  static constexpr int B4 = lg::best_pitch(E2, D, NT, false, 4, R0B, PAIRB);
+  static constexpr int B3 = lg::best_pitch(E2, D, NT, false, 3, R0B, PAIRB);
   static constexpr int LA = lg::pick_layout(A5, A4, A3), LB = lg::pick_layout(B5, B4, B3);
   static constexpr int PA = LA & 0xffff, PB = LB & 0xffff;  // line pitches (slots)
   static constexpr int SA = LA >> 16, SB = LB >> 16;        // padding periods (log2)
@@ -619,11 +630,10 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
       }
     }
   } else {
-    // r2c: every pass on chip (the last one with the lanes across the rows), then the split of
-    // each row pair into X_k and X_{m-k}
+    // r2c: every pass but the last on chip, then the last pass and the split of each row pair
+    // into X_k and X_{m-k}
     constexpr int NPB = lg::np(E2, Cf::R0B);
     lg_middles<E2, Cf::R0B, D, NT, PB, SB, 1, NPB - 1>(sm, tw);
-    lg_pass_across<E2, Cf::R0B, NPB - 1, D, NT, PB, SB>(sm, tw);
     constexpr int64_t M = int64_t(N1) * N2;
     constexpr int H = D / 2;
     const float2 *lo2 = reinterpret_cast<const float2 *>(a.lo2), *hi2 = reinterpret_cast<const float2 *>(a.hi2);
@@ -633,26 +643,58 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
       asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x * fct), "f"(vy), "l"(pol)
                    : "memory");
     };
-    auto split = [&](int la, int pa, int lb, int pb, int64_t ka, bool two) {
-      const float2 za = sm[la * PB + lg::spad(pa, SB)], zc = cj<float>(sm[lb * PB + lg::spad(pb, SB)]);
+    // X_ka and (two) X_{m-ka} from za = Z_ka and zb = Z_{m-ka}
+    auto split = [&](float2 za, float2 zb, int64_t ka, bool two) {
+      const float2 zc = cj<float>(zb);
       const float2 Ev = scl<float>(add<float>(za, zc), 0.5f);
       const float2 O = mnegi<float>(scl<float>(sub<float>(za, zc), 0.5f));
       const float2 t = mul<float>(split_twiddle<float>(lo2, hi2, a.shift2, uint32_t(ka)), O);
       put(ka, add<float>(Ev, t));
       if (two) put(M - ka, cj<float>(sub<float>(Ev, t)));
     };
-    // H divides NT: a thread keeps its line pair i and steps through positions
-    constexpr int SPLIT_IT = H * N2 / NT;
-    static_assert((H * N2) % NT == 0 && NT % H == 0, "whole split iterations");
+    if (part != 0) {
+      // The last pass straight into the split: lane l < 16 of a warp runs butterfly j of primary
+      // line i, lane l + 16 butterfly NS-1-j of the mirror line D-1-i, whose output R-1-k is the
+      // mirror element (index m - k) of the lane's output k. Each lane splits the pairs of its
+      // outputs k < R/2; the partner's half comes by shuffle (no shared-memory round trip and
+      // no barrier). The layout's pitch is chosen for this pattern (LgCfg::PAIRB).
+      constexpr int P = NPB - 1, R = lg::radix(E2, Cf::R0B, P), NS = N2 / R;
+      constexpr int WARPS = NT / 32, ITER = H * NS / (WARPS * 16);
+      static_assert((H * NS) % (WARPS * 16) == 0 && R % 2 == 0, "whole pair iterations");
+      const int lane = int(threadIdx.x) & 31;
+      const bool mir = lane >= 16;
+      for (int it = 0; it < ITER; ++it) {
+        const int v = ((int(threadIdx.x) >> 5) + it * WARPS) * 16 + (lane & 15);
+        const int i = v % H, j = v / H;
+        const int line = mir ? D - 1 - i : i, jj = mir ? NS - 1 - j : j;
+        float2 z[R];
+        lg_last_one<E2, Cf::R0B, PB, SB>(sm, tw, line, jj, z);
+        const int64_t kb = pair_index<N1, D>(part, line) + int64_t(N1) * jj;
+#pragma unroll
+        for (int k = 0; k < R / 2; ++k) {
+          const float2 zb = make_float2(__shfl_xor_sync(0xffffffffu, z[R - 1 - k].x, 16),
+                                        __shfl_xor_sync(0xffffffffu, z[R - 1 - k].y, 16));
+          split(z[k], zb, kb + int64_t(N1) * NS * k, true);
+        }
+      }
+    } else {
+      // tile 0 (rows 0 and n1/2 mirror onto themselves): the last pass in place with the lanes
+      // across the rows, then the split from shared memory
+      lg_pass_across<E2, Cf::R0B, NPB - 1, D, NT, PB, SB>(sm, tw);
+      auto at = [&](int l, int pos) { return sm[l * PB + lg::spad(pos, SB)]; };
+      // H divides NT: a thread keeps its line pair i and steps through positions
+      constexpr int SPLIT_IT = H * N2 / NT;
+      static_assert((H * N2) % NT == 0 && NT % H == 0, "whole split iterations");
 #pragma unroll 4
-    for (int it = 0; it < SPLIT_IT; ++it) {
-      const int u = int(threadIdx.x) + it * NT;
-      const int i = u % H, k2 = u / H;
-      int la, pa, lb, pb;
-      pair_unit<D, N2>(part, i, k2, la, pa, lb, pb);
-      split(la, pa, lb, pb, pair_index<N1, D>(part, la) + int64_t(N1) * pa, true);
+      for (int it = 0; it < SPLIT_IT; ++it) {
+        const int u = int(threadIdx.x) + it * NT;
+        const int i = u % H, k2 = u / H;
+        int la, pa, lb, pb;
+        pair_unit<D, N2>(0, i, k2, la, pa, lb, pb);
+        split(at(la, pa), at(lb, pb), pair_index<N1, D>(0, la) + int64_t(N1) * pa, true);
+      }
+      if (threadIdx.x == 0) split(at(0, N2 / 2), at(0, N2 / 2), M / 2, false);
     }
-    if (part == 0 && threadIdx.x == 0) split(0, N2 / 2, 0, N2 / 2, M / 2, false);
   }
 }
 
