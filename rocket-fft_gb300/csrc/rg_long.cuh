@@ -45,9 +45,9 @@
 // 1 .. D/2-1 with their mirrors) and stores X_k and X_{m-k} from each pair: past tile 0 the last
 // pass runs a row's butterfly and the mirror row's mirrored butterfly in lanes l and l + 16 of
 // one warp, which exchange their halves by shuffle; tile 0 splits from shared memory. c2r is
-// the mirror image: its phase-A tile holds columns j2 and n2 - j2, merges the
-// Hermitian half spectrum into conj(Z) as it loads, and phase B stores conj of the result as
-// the real pairs.
+// the mirror image: its phase-A tile holds columns j2 and n2 - j2, merges the Hermitian half
+// spectrum into conj(Z) as it loads (past tile 0 in the first pass's registers, the same lane
+// pairing), and phase B stores conj of the result as the real pairs.
 #pragma once
 #include "rg_fixed_kernel.cuh"
 
@@ -191,10 +191,12 @@ constexpr int first_radix(int kind, int E1, int E2, bool phase_a) {
   return phase_a ? ra : rb;
 }
 
-// pair_last: the last pass of the r2c phase B instead (lg_phase_b): lane l < 16 of a warp on
-// primary line i at butterfly j, lane l + 16 on the mirror line M-1-i at butterfly NS-1-j.
-constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, int r0, bool pair_last) {
+// pair: the real transforms' paired lines instead, for phase A's first pass (c2r, a_side) or
+// phase B's last pass (r2c): lane l < 16 of a warp on primary line i at butterfly j, lane l + 16
+// on the mirror line M-1-i at the mirrored butterfly.
+constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, int r0, bool pair) {
   const int L = 1 << E, NP = np(E, r0);
+  const bool pair_first = pair && a_side, pair_last = pair && !a_side;
   int total = 0;
   for (int w = 0; w < NT / 32 && w < 4; ++w) {
     int slot[32] = {};
@@ -203,7 +205,12 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
       for (int k = 0; k < r0; ++k) {
         for (int l = 0; l < 32; ++l) {
           const int u = 32 * w + l + it * NT;
-          const int line = a_side ? u % M : u / (L / r0), j = a_side ? u / M : u % (L / r0);
+          int line = a_side ? u % M : u / (L / r0), j = a_side ? u / M : u % (L / r0);
+          if (pair_first) {
+            const int v = (w + it * (NT / 32)) * 16 + (l & 15), i = v % (M / 2), jj = v / (M / 2);
+            line = l >= 16 ? M - 1 - i : i;
+            j = l >= 16 ? L / r0 - 1 - jj : jj;
+          }
           slot[l] = line * pitch + spad(r0 * j + k, ps);
         }
         total += wave(slot);
@@ -239,11 +246,11 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
 }
 // For padding period 2^ps: the pitch (>= the padded line length, within 16 slots of it) with
 // the fewest wavefronts, as cost * 2^16 + pitch.
-constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps, int r0, bool pair_last = false) {
+constexpr int best_pitch(int E, int M, int NT, bool a_side, int ps, int r0, bool pair = false) {
   const int base = spad((1 << E) - 1, ps) + 1;
   int best = base, cost = 1 << 14;
   for (int p = base; p < base + 16; ++p) {
-    const int c = phase_waves(E, M, NT, p, a_side, ps, r0, pair_last);
+    const int c = phase_waves(E, M, NT, p, a_side, ps, r0, pair);
     if (c < cost) {
       cost = c;
       best = p;
@@ -274,8 +281,10 @@ template <int E1, int E2, int ET, int KIND> struct LgCfg {
   static constexpr int MINB = RMAX == 32 ? 512 / NT : 1024 / NT;
   // shared layout of each phase: padding period and line pitch (each candidate period searched
   // in a constant of its own, within the compiler's constant-evaluation budget)
-  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5, R0A), A4 = lg::best_pitch(E1, C, NT, true, 4, R0A);
-  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3, R0A);
+  static constexpr bool PAIRA = KIND == LG_C2R;  // c2r: phase A's first pass on column pairs
+  static constexpr int A5 = lg::best_pitch(E1, C, NT, true, 5, R0A, PAIRA);
+  static constexpr int A4 = lg::best_pitch(E1, C, NT, true, 4, R0A, PAIRA);
+  static constexpr int A3 = lg::best_pitch(E1, C, NT, true, 3, R0A, PAIRA);
   static constexpr bool PAIRB = KIND == LG_R2C;  // r2c: phase B's last pass on line pairs
   static constexpr int B5 = lg::best_pitch(E2, D, NT, false, 5, R0B, PAIRB);
   static constexpr int B4 = lg::best_pitch(E2, D, NT, false, 4, R0B, PAIRB);
@@ -495,7 +504,7 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
     lg_middles<E1, Cf::R0A, C, NT, PA, SA, 1, lg::np(E1, Cf::R0A) - 1>(sm, tw);
   } else {
     // c2r: merge the half spectrum X (m + 1 elements, m = n1 n2) of columns j2 and n2 - j2
-    // into conj(Z) on chip, then every pass but the last in shared memory
+    // into conj(Z) on chip, then every pass but the last
     constexpr int64_t M = int64_t(N1) * N2;
     constexpr int H = C / 2;
     const float2 *lo2 = reinterpret_cast<const float2 *>(a.lo2), *hi2 = reinterpret_cast<const float2 *>(a.hi2);
@@ -508,32 +517,73 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       if (j == 0 || j == M) v.y = 0.f;
       return v;
     };
-    // conj(Z_ja) = conj(A + u), conj(Z_{m-ja}) = A - u,  A = X_ja + conj X_{m-ja},
+    // conj(Z_ja) = conj(A + u) into za, conj(Z_{m-ja}) = A - u into zb,  A = X_ja + conj X_{m-ja},
     // u = i (X_ja - conj X_{m-ja}) conj(W_2m^ja)
-    auto merge = [&](int la, int pa, int lb, int pb, int64_t ja, bool two) {
+    auto merge = [&](int64_t ja, float2 &za, float2 &zb) {
       const float2 xa = ldX(ja), xb = ldX(M - ja);
       const float2 A = add<float>(xa, cj<float>(xb)), B = sub<float>(xa, cj<float>(xb));
       const float2 w = split_twiddle<float>(lo2, hi2, a.shift2, uint32_t(ja));
       const float2 uu = mposi<float>(mulc<float>(B, w));
-      sm[la * PA + lg::spad(pa, SA)] = cj<float>(add<float>(A, uu));
-      if (two) sm[lb * PA + lg::spad(pb, SA)] = sub<float>(A, uu);
+      za = cj<float>(add<float>(A, uu));
+      zb = sub<float>(A, uu);
     };
     const int t = part;
-    constexpr int MERGE_IT = H * N1 / NT;
-    static_assert((H * N1) % NT == 0 && NT % H == 0, "whole merge iterations");
+    if (t != 0) {
+      // The merge straight into the first pass: lane l < 16 of a warp runs butterfly j of primary
+      // column line i, lane l + 16 butterfly LR-1-j of the mirror line C-1-i, whose input R-1-k
+      // is the mirror element (index m - j) of the lane's input k. Each lane merges the pairs of
+      // its inputs k < R/2 and hands the partner its half by shuffle (no shared-memory round trip
+      // and no barrier before the pass). The layout's pitch is chosen for this pattern
+      // (LgCfg::PAIRA).
+      constexpr int R = Cf::R0A, LR = N1 / R;
+      constexpr int WARPS = NT / 32, ITER = H * LR / (WARPS * 16);
+      static_assert((H * LR) % (WARPS * 16) == 0 && R % 2 == 0, "whole pair iterations");
+      const int lane = int(threadIdx.x) & 31;
+      const bool mir = lane >= 16;
+      for (int it = 0; it < ITER; ++it) {
+        const int v = ((int(threadIdx.x) >> 5) + it * WARPS) * 16 + (lane & 15);
+        const int i = v % H, j = v / H;
+        const int line = mir ? C - 1 - i : i, jj = mir ? LR - 1 - j : j;
+        const int64_t jb = int64_t(jj) * N2 + pair_index<N2, C>(t, line);
+        float2 z[R];
+#pragma unroll
+        for (int k = 0; k < R / 2; ++k) merge(jb + int64_t(k) * LR * N2, z[k], z[R - 1 - k]);
+        // z[R-1-k] (k < R/2) holds the partner's input R-1-k: swap those halves
+#pragma unroll
+        for (int k = R / 2; k < R; ++k) {
+          z[k].x = __shfl_xor_sync(0xffffffffu, z[k].x, 16);
+          z[k].y = __shfl_xor_sync(0xffffffffu, z[k].y, 16);
+        }
+        dft<float, R>(z);
+        float2 *l0 = sm + line * PA;
+#pragma unroll
+        for (int k = 0; k < R; ++k) l0[lg::sp_k<1, SA>(jj * R, k)] = z[k];
+      }
+      __syncthreads();
+    } else {
+      // tile 0 (columns 0 and n2/2 mirror onto themselves): merge into shared memory, then the
+      // first pass with the lanes across the columns
+      auto merge_sm = [&](int la, int pa, int lb, int pb, int64_t ja, bool two) {
+        float2 za, zb;
+        merge(ja, za, zb);
+        sm[la * PA + lg::spad(pa, SA)] = za;
+        if (two) sm[lb * PA + lg::spad(pb, SA)] = zb;
+      };
+      constexpr int MERGE_IT = H * N1 / NT;
+      static_assert((H * N1) % NT == 0 && NT % H == 0, "whole merge iterations");
 #pragma unroll 4
-    for (int it = 0; it < MERGE_IT; ++it) {
-      const int u = int(threadIdx.x) + it * NT;
-      const int i = u % H, j1 = u / H;
-      int la, pa, lb, pb;
-      pair_unit<C, N1>(t, i, j1, la, pa, lb, pb);
-      const int64_t ja = int64_t(pa) * N2 + pair_index<N2, C>(t, la);
-      merge(la, pa, lb, pb, ja, ja != 0);
+      for (int it = 0; it < MERGE_IT; ++it) {
+        const int u = int(threadIdx.x) + it * NT;
+        const int i = u % H, j1 = u / H;
+        int la, pa, lb, pb;
+        pair_unit<C, N1>(0, i, j1, la, pa, lb, pb);
+        const int64_t ja = int64_t(pa) * N2 + pair_index<N2, C>(0, la);
+        merge_sm(la, pa, lb, pb, ja, ja != 0);
+      }
+      if (threadIdx.x == 0) merge_sm(0, N1 / 2, 0, N1 / 2, M / 2, false);
+      __syncthreads();
+      lg_pass_across<E1, Cf::R0A, 0, C, NT, PA, SA>(sm, tw);
     }
-    if (t == 0 && threadIdx.x == 0) merge(0, N1 / 2, 0, N1 / 2, M / 2, false);
-    __syncthreads();
-    // the first pass with the lanes across the columns, the rest along them
-    lg_pass_across<E1, Cf::R0A, 0, C, NT, PA, SA>(sm, tw);
     lg_middles<E1, Cf::R0A, C, NT, PA, SA, 1, lg::np(E1, Cf::R0A) - 1>(sm, tw);
   }
   // last pass: outputs k1 = j + k * NS, times W_n^{j2 k1}, to Y[k1][j2]; lanes across the C
