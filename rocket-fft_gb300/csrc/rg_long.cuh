@@ -84,6 +84,17 @@ namespace lg {
 // chosen per phase together with the line pitch)
 __host__ __device__ constexpr int spad(int pos, int ps) { return pos + (pos >> ps); }
 
+// The real transforms' paired passes (the r2c split after phase B's last pass, the c2r merge
+// before phase A's first): lane l of warp w, iteration it, in a tile of `lines` lines with `nb`
+// butterflies each. Lane l < 16 takes primary line i at butterfly j, lane l + 16 the mirror
+// line lines-1-i at butterfly nb-1-j, so that output (r2c) or input (c2r) R-1-k of the one is
+// the mirror element of the other's k.
+__host__ __device__ constexpr void pair_lane(int w, int it, int warps, int l, int lines, int nb, int &line, int &j) {
+  const int h = lines / 2, v = (w + it * warps) * 16 + (l & 15), i = v % h, q = v / h;
+  line = l >= 16 ? lines - 1 - i : i;
+  j = l >= 16 ? nb - 1 - q : q;
+}
+
 // spad(base + k * STEP, PS) as the base's index plus a compile-time offset, for the runs the
 // passes use: STEP a multiple of 2^PS (any base); STEP 16 with PS 5 and base % 32 < 16; STEP 1
 // with base a multiple of 16 (the first-pass writes, base = 16 j, k < 16); else spad().
@@ -206,11 +217,7 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
         for (int l = 0; l < 32; ++l) {
           const int u = 32 * w + l + it * NT;
           int line = a_side ? u % M : u / (L / r0), j = a_side ? u / M : u % (L / r0);
-          if (pair_first) {
-            const int v = (w + it * (NT / 32)) * 16 + (l & 15), i = v % (M / 2), jj = v / (M / 2);
-            line = l >= 16 ? M - 1 - i : i;
-            j = l >= 16 ? L / r0 - 1 - jj : jj;
-          }
+          if (pair_first) pair_lane(w, it, NT / 32, l, M, L / r0, line, j);
           slot[l] = line * pitch + spad(r0 * j + k, ps);
         }
         total += wave(slot);
@@ -223,11 +230,7 @@ constexpr int phase_waves(int E, int M, int NT, int pitch, bool a_side, int ps, 
             const int u = 32 * w + l + it * NT;
             const bool last = p == NP - 1;
             int line = last ? u % M : u / LR, j = last ? u / M : u % LR;
-            if (last && pair_last) {
-              const int v = (w + it * (NT / 32)) * 16 + (l & 15), i = v % (M / 2), jj = v / (M / 2);
-              line = l >= 16 ? M - 1 - i : i;
-              j = l >= 16 ? NS - 1 - jj : jj;
-            }
+            if (last && pair_last) pair_lane(w, it, NT / 32, l, M, NS, line, j);
             slot[l] = line * pitch + spad(j + k * LR, ps);
           }
           total += wave(slot);
@@ -413,7 +416,7 @@ __device__ __forceinline__ void lg_last_one(const float2 *sm, const float2 *__re
 // [0, H) are the rows (or columns) t H + l, line LINES-1-i their mirror NL - (t H + i); tile 0
 // holds 0 .. H-1, its mirrors NL-1 .. NL-H+1 on lines LINES-2 .. H, and NL/2 on line LINES-1.
 template <int NL, int LINES>
-__device__ __forceinline__ int pair_index(int t, int l) {
+__host__ __device__ __forceinline__ int pair_index(int t, int l) {
   constexpr int H = LINES / 2;
   if (l < H) return t * H + l;
   if (t == 0 && l == LINES - 1) return NL / 2;
@@ -538,12 +541,9 @@ __device__ __forceinline__ void lg_phase_a(const LongArgs &a, float2 *sm, const 
       constexpr int R = Cf::R0A, LR = N1 / R;
       constexpr int WARPS = NT / 32, ITER = H * LR / (WARPS * 16);
       static_assert((H * LR) % (WARPS * 16) == 0 && R % 2 == 0, "whole pair iterations");
-      const int lane = int(threadIdx.x) & 31;
-      const bool mir = lane >= 16;
       for (int it = 0; it < ITER; ++it) {
-        const int v = ((int(threadIdx.x) >> 5) + it * WARPS) * 16 + (lane & 15);
-        const int i = v % H, j = v / H;
-        const int line = mir ? C - 1 - i : i, jj = mir ? LR - 1 - j : j;
+        int line, jj;
+        lg::pair_lane(int(threadIdx.x) >> 5, it, WARPS, int(threadIdx.x) & 31, C, LR, line, jj);
         const int64_t jb = int64_t(jj) * N2 + pair_index<N2, C>(t, line);
         float2 z[R];
 #pragma unroll
@@ -711,12 +711,9 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
       constexpr int P = NPB - 1, R = lg::radix(E2, Cf::R0B, P), NS = N2 / R;
       constexpr int WARPS = NT / 32, ITER = H * NS / (WARPS * 16);
       static_assert((H * NS) % (WARPS * 16) == 0 && R % 2 == 0, "whole pair iterations");
-      const int lane = int(threadIdx.x) & 31;
-      const bool mir = lane >= 16;
       for (int it = 0; it < ITER; ++it) {
-        const int v = ((int(threadIdx.x) >> 5) + it * WARPS) * 16 + (lane & 15);
-        const int i = v % H, j = v / H;
-        const int line = mir ? D - 1 - i : i, jj = mir ? NS - 1 - j : j;
+        int line, jj;
+        lg::pair_lane(int(threadIdx.x) >> 5, it, WARPS, int(threadIdx.x) & 31, D, NS, line, jj);
         float2 z[R];
         lg_last_one<E2, Cf::R0B, PB, SB>(sm, tw, line, jj, z);
         const int64_t kb = pair_index<N1, D>(part, line) + int64_t(N1) * jj;

@@ -1,6 +1,7 @@
 """Host-compiled checks of device code (no GPU needed): the radix butterflies of the on-chip FFT
-against a naive long-double DFT, and the compile-time pass schedule of the fixed-length
-kernels against the host core plan."""
+against a naive long-double DFT, the compile-time pass schedule of the fixed-length
+kernels against the host core plan, and the long kernel's lane pairing of the real transforms'
+mirror rows and columns (coverage, mirror partners, conflict-free shared reads)."""
 
 from __future__ import annotations
 
@@ -36,6 +37,16 @@ def test_fixed_schedule(tmp_path):
     r = subprocess.run([_nvcc(), "-O1", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
                         f"-I{ROOT / 'include'}", str(HERE / "native" / "fixed_schedule.cu"),
                         str(PKG_DIR / "csrc" / "rg_plan.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_long_pairs(tmp_path):
+    exe = tmp_path / "long_pairs"
+    r = subprocess.run([_nvcc(), "-O1", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
+                        f"-I{ROOT / 'include'}", str(HERE / "native" / "long_pairs.cu"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
