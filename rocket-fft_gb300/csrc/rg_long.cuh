@@ -748,7 +748,7 @@ __device__ __forceinline__ void lg_phase_b(const LongArgs &a, float2 *sm, const 
 // ---- the persistent kernel ----
 
 // Ticket block -> (group, phase), for lookahead `look` (0 <= look <= ng).
-__device__ __forceinline__ void lg_decode(int blk, int ng, int look, int &g, bool &isA) {
+__host__ __device__ __forceinline__ void lg_decode(int blk, int ng, int look, int &g, bool &isA) {
   if (blk < look) {
     g = blk;
     isA = true;

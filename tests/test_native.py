@@ -1,7 +1,9 @@
 """Host-compiled checks of device code (no GPU needed): the radix butterflies of the on-chip FFT
 against a naive long-double DFT, the compile-time pass schedule of the fixed-length
-kernels against the host core plan, and the long kernel's lane pairing of the real transforms'
-mirror rows and columns (coverage, mirror partners, conflict-free shared reads)."""
+kernels against the host core plan, the long kernel's lane pairing of the real transforms'
+mirror rows and columns (coverage, mirror partners, conflict-free shared reads), and its tile
+schedule (ticket order, waits on lower tickets only, ring-slot exclusion, no deadlock under random
+interleavings of persistent CTAs)."""
 
 from __future__ import annotations
 
@@ -47,6 +49,16 @@ def test_long_pairs(tmp_path):
     exe = tmp_path / "long_pairs"
     r = subprocess.run([_nvcc(), "-O1", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
                         f"-I{ROOT / 'include'}", str(HERE / "native" / "long_pairs.cu"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_long_tickets(tmp_path):
+    exe = tmp_path / "long_tickets"
+    r = subprocess.run([_nvcc(), "-O1", "-std=c++17", "--expt-relaxed-constexpr", f"-I{PKG_DIR / 'csrc'}",
+                        f"-I{ROOT / 'include'}", str(HERE / "native" / "long_tickets.cu"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
